@@ -1,0 +1,221 @@
+/*
+ * h3d -- GB300-native 3D frequency-domain Helmholtz hot path (27-point stencil with PML).
+ *
+ * Plain C ABI: plain pointers and sizes, no C++ or framework types.  Complex
+ * device vectors are interleaved (re, im) pairs of double (H3D_C128) or float
+ * (H3D_C64), column-major over the grid (x fastest, idx = i + j*nx + k*nx*ny)
+ * with right-hand side s at offset s*N.  Wavenumber arrays hold N real values
+ * (plus an optional imaginary plane for complex frequencies).
+ *
+ * Entry points and the reference interface each one replaces
+ * (paths inside the reference project SLIM-release-apps):
+ *
+ *   h3d_mvp            Helm3dmvp_{forw,adj}[_wnc|_deriv]_mex
+ *                      (tools/algorithms/3DFreqModeling/Helm3dmvp_mex.c:58-107,
+ *                       dispatch helm3d_operto27_mvp.m:22-42)
+ *   h3d_kacz_sweep     Helm3d_kacz_sweep{,_wnc,_adj}_mex
+ *                      (tools/algorithms/3DFreqModeling/Helm3dkaczswp_mex.c:123-199,
+ *                       dispatch helm3d_operto27_kaczswp.m:20-30)
+ *   h3d_mex_mvp,       the same two gateways with MATLAB's host-side argument list
+ *   h3d_mex_kacz_sweep (separate real/imag double planes, n and npml as doubles);
+ *                      used by the drop-in MEX gateway
+ *   h3d_solve          H\b and H'\b through linearsolve + CGMN with the Kaczmarz
+ *                      preconditioner (tools/solvers/Krylov/linearsolve.m:148-168,
+ *                      CGMN.m:36-94, opAbstractMatrix.m:117-125)
+ *   h3d_solve_batch    many (problem, right-hand side) solves of uneven size in one launch
+ *                      sequence (the (src,freq) loop of PDEfunc.m:254-347 batched)
+ *   h3d_grad_accum     T_adj(z,u) = conj(u).*(dH'*z) summed over sources and cropped to the
+ *                      physical grid (discrete_helmholtz.m:288, PDEfunc.m:386,394)
+ *   h3d_src_inject,    sinc-Kaiser source injection Ps and receiver sampling Pr
+ *   h3d_rec_sample,    (opInterp.m:34-58, opSincInterp.m:26-70, DataGrid.m:22-44)
+ *   h3d_rec_spread
+ *
+ * Every call is asynchronous on the given CUDA stream (NULL = legacy default
+ * stream) unless documented otherwise; all pointers are device pointers unless
+ * the function name says "mex"/"host".  The library keeps no state between calls
+ * except cached device properties and the kernels' constant tables.
+ */
+#ifndef H3D_H
+#define H3D_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define H3D_API_VERSION 1
+
+/* Status codes.  The reference reports errors with mexErrMsgIdAndTxt
+ * (Helm3dmvp_mex.c:75-85, Helm3dkaczswp_mex.c:143-164); h3d_status_id() maps a
+ * code to the matching reference error identifier. */
+typedef enum {
+    H3D_OK = 0,
+    H3D_ERR_NSIZE = 1,          /* n must be a 3-length vector of positive sizes */
+    H3D_ERR_XSIZE = 2,          /* x must have nx*ny*nz rows */
+    H3D_ERR_BSIZE = 3,          /* b must have nx*ny*nz rows */
+    H3D_ERR_BAD_ARG = 4,        /* other invalid argument (NULL pointer, bad mode, w out of (0,2), ...) */
+    H3D_ERR_NOT_CONVERGED = 5,  /* solver hit maxit before the tolerance */
+    H3D_ERR_TIMEOUT = 6,        /* a bounded device-side wait expired */
+    H3D_ERR_CUDA = 7,           /* CUDA runtime error (message via h3d_last_error) */
+    H3D_ERR_NO_MEMORY = 8,
+    H3D_ERR_NONFINITE = 9       /* NaN/Inf met in the iteration */
+} h3d_status;
+
+typedef enum { H3D_C128 = 0, H3D_C64 = 1 } h3d_dtype;
+typedef enum { H3D_FORWARD = 1, H3D_ADJOINT = 2 } h3d_mode;
+
+/* Kaczmarz row orderings of one double sweep.
+ *  LEX       the reference's lexicographic order (k, j, i ascending, then descending):
+ *            bit-compatible with Helm3d_kacz_sweep_mex.  Executed as hyperplane
+ *            wavefronts t = i + 3j + 9k (no two rows on a plane share a neighbour,
+ *            and every pair of rows that does is ordered as in the reference).
+ *  COLOUR27  27 colour classes q = (i%3) + 3(j%3) + 9(k%3), ascending then descending.
+ *  BLOCK     blocks of block[0..2] points visited by the block wavefront
+ *            T = I + 2J + 4K, COLOUR27 order inside each block.
+ * All three give a symmetric double sweep, hence a Hermitian positive
+ * semi-definite I - Q for CGMN; they differ in the iterates, not the solution. */
+typedef enum { H3D_ORDER_LEX = 0, H3D_ORDER_COLOUR27 = 1, H3D_ORDER_BLOCK = 2 } h3d_order;
+
+typedef enum { H3D_PREC_FP64 = 0, H3D_PREC_MIXED = 1 } h3d_precision;
+
+/* Stopping rules.  PRECONDITIONED is CGMN.m:79 (max over columns of the
+ * preconditioned residual ratio <= tol); TRUE_RESIDUAL requires
+ * ||b - H u||_2 / ||b||_2 <= tol for every right-hand side. */
+typedef enum { H3D_STOP_PRECONDITIONED = 0, H3D_STOP_TRUE_RESIDUAL = 1 } h3d_stop_rule;
+
+typedef struct h3d_grid {
+    int32_t n[3];     /* nx, ny, nz including the PML */
+    double h[3];      /* grid spacing hx, hy, hz */
+    int32_t npml[6];  /* lo_x, hi_x, lo_y, hi_y, lo_z, hi_z: the reference's 2x3 npml, column-major */
+} h3d_grid;
+
+typedef struct h3d_solve_opts {
+    double tol;             /* default 1e-6 (LinSolveOpts.m:56) */
+    int32_t maxit;          /* default 10000 (LinSolveOpts.m:57); inner iterations cap */
+    double w;               /* relaxation, default 1.5 (linearsolve.m:150) */
+    int32_t precision;      /* h3d_precision */
+    int32_t order;          /* h3d_order */
+    int32_t stop_rule;      /* h3d_stop_rule */
+    int32_t check_every;    /* iterations between host-visible convergence checks (graph length) */
+    double inner_tol;       /* MIXED: relative tolerance of each complex64 inner solve */
+    int32_t max_outer;      /* MIXED: maximum refinement steps */
+    int32_t block[3];       /* BLOCK order: block size (0 = choose automatically) */
+    int32_t use_graphs;     /* capture the iteration in a CUDA graph (1) or launch eagerly (0) */
+    int32_t verbose;        /* print progress to stderr */
+} h3d_solve_opts;
+
+typedef struct h3d_solve_info {
+    int32_t iters;          /* CGMN iterations (max over right-hand sides; summed over refinement steps) */
+    int32_t outer;          /* refinement steps (MIXED) or true-residual restarts */
+    int32_t converged;      /* 1 if every right-hand side met the stopping rule */
+    int32_t nrhs;
+    double rel_res_true;    /* max over RHS of ||b - H u|| / ||b|| (FP64), or -1 if not computed */
+    double rel_res_prec;    /* max over RHS of the last preconditioned residual ratio */
+    double seconds;         /* wall time of the call (host clock, after stream sync) */
+    double sweep_seconds;   /* device time in sweep kernels, if measured (else 0) */
+} h3d_solve_info;
+
+/* One problem of a batched solve: its own grid, wavenumber and right-hand sides. */
+typedef struct h3d_problem {
+    h3d_grid grid;
+    const double *wn_re;    /* device, N values */
+    const double *wn_im;    /* device or NULL */
+    const void *b;          /* device, complex128 interleaved, N x nrhs */
+    void *u;                /* device, complex128 interleaved, N x nrhs (output) */
+    int32_t nrhs;
+    int32_t mode;           /* h3d_mode */
+} h3d_problem;
+
+/* ---- library ----------------------------------------------------------------------- */
+int h3d_version(void);
+const char *h3d_status_id(int status);      /* reference-style error identifier */
+const char *h3d_last_error(void);           /* message of the last failing call on this thread */
+void h3d_default_opts(h3d_solve_opts *opts);
+
+/* ---- operator application ------------------------------------------------------------ */
+/* y = H x (mode FORWARD), H^H x (ADJOINT); deriv != 0 applies dH (the mass term only,
+ * Helm3d_27pt.h:202-206) with wn holding dwn.  wn_re/wn_im are double for H3D_C128 and
+ * float for H3D_C64; wn_im may be NULL.  x and y: N x nrhs, must not overlap. */
+int h3d_mvp(const h3d_grid *g, const void *wn_re, const void *wn_im, const void *x, void *y,
+            int nrhs, int mode, int deriv, int dtype, void *stream);
+
+/* One forward + backward Kaczmarz sweep with relaxation w on x (in place), right-hand
+ * side b (NULL = 0).  Same element types as h3d_mvp. */
+int h3d_kacz_sweep(const h3d_grid *g, const void *wn_re, const void *wn_im, double w, void *x,
+                   const void *b, int nrhs, int mode, int order, const int32_t *block, int dtype,
+                   void *stream);
+
+/* r = b - H x (FP64 residual for iterative refinement), and per-RHS ||r||^2, ||b||^2
+ * written to device arrays rr2/bb2 (nrhs doubles each; either may be NULL). */
+int h3d_residual(const h3d_grid *g, const double *wn_re, const double *wn_im, const void *b,
+                 const void *x, void *r, double *rr2, double *bb2, int nrhs, int mode,
+                 void *stream);
+
+/* ---- MATLAB-layout host entry points (what the drop-in MEX gateway calls) ----------- */
+/* Arguments exactly as the reference gateways receive them: wn (N, re/im planes; im may
+ * be NULL), h[3], n[3] and npml[6] as doubles, x split into re/im planes (im may be
+ * NULL), nrhs columns.  Outputs are split planes of N*nrhs doubles.  Synchronous. */
+int h3d_mex_mvp(const double *wn_re, const double *wn_im, const double *h, const double *n,
+                size_t n_len, const double *npml, const double *x_re, const double *x_im,
+                size_t x_rows, double *y_re, double *y_im, int mode, int deriv);
+int h3d_mex_kacz_sweep(const double *wn_re, const double *wn_im, const double *h,
+                       const double *n, size_t n_len, const double *npml, double w,
+                       const double *x_re, const double *x_im, size_t x_rows, size_t nrhs,
+                       const double *b_re, const double *b_im, size_t b_rows, double *y_re,
+                       double *y_im, int mode, int order);
+
+/* ---- solvers -------------------------------------------------------------------------- */
+/* u = H \ b (mode FORWARD) or H^H \ b (ADJOINT), complex128 interleaved device vectors,
+ * N x nrhs.  Right-hand sides with ||b|| < 1e-12 return u = 0 (opAbstractMatrix.m:118).
+ * iters_per_rhs (device or NULL, nrhs ints) receives each column's iteration count;
+ * res_hist (host or NULL) receives up to res_hist_len preconditioned residual ratios
+ * (max over columns) sampled every check_every iterations. */
+int h3d_solve(const h3d_grid *g, const double *wn_re, const double *wn_im, const void *b,
+              void *u, int nrhs, int mode, const h3d_solve_opts *opts, h3d_solve_info *info,
+              double *res_hist, int res_hist_len, void *stream);
+
+/* Solve every problem of the table; infos (host, nprob entries) may be NULL. */
+int h3d_solve_batch(const h3d_problem *probs, int nprob, const h3d_solve_opts *opts,
+                    h3d_solve_info *infos, void *stream);
+
+/* Same as h3d_solve with host (pinned or pageable) b/u and wavenumber: the
+ * host->device copies, the solve and the device->host copy of u all happen
+ * inside the call.  Synchronous. */
+int h3d_solve_host(const h3d_grid *g, const double *wn_re, const double *wn_im,
+                   const void *b_host, void *u_host, int nrhs, int mode,
+                   const h3d_solve_opts *opts, h3d_solve_info *info);
+
+/* ---- FWI pieces ----------------------------------------------------------------------- */
+/* g_phys[p] += scale * sum_s Re( conj(u_s[i]) * dH^H z_s [i] ) for the physical points i
+ * (the PML is cropped, cut_pml=true: discrete_helmholtz.m:231-232).  dwn is the
+ * derivative of the wavenumber (device, N doubles); g_phys has (nx-lo_x-hi_x) *
+ * (ny-...) * (nz-...) doubles. */
+int h3d_grad_accum(const h3d_grid *g, const double *dwn, const void *u, const void *z,
+                   int nrhs, double scale, double *g_phys, void *stream);
+
+/* Separable sinc x Kaiser(r=4, beta=6.31) weights: for point p (coords in grid units
+ * of the computational grid, 0-based, nsrc points), w[p][a][0..8] are the weights of
+ * grid indices base[p][a] + 0..8 along axis a (weights outside the grid are zero). */
+int h3d_sinc_weights(const h3d_grid *g, const double *pts, int npts, int32_t *base,
+                     double *w);
+
+/* b_s += scale_s * Ps(point s)   (complex scale per source; pts: host weights from
+ * h3d_sinc_weights copied to device). */
+int h3d_src_inject(const h3d_grid *g, const int32_t *base, const double *w, const double *scale,
+                   void *b, int nsrc, void *stream);
+
+/* d[r + s*nrec] = (Pr u_s)[r]   (receiver sampling, complex128). */
+int h3d_rec_sample(const h3d_grid *g, const int32_t *base, const double *w, int nrec,
+                   const void *u, int nrhs, void *d, void *stream);
+
+/* b_s = scale * Pr^T d_s   (adjoint source; b is overwritten). */
+int h3d_rec_spread(const h3d_grid *g, const int32_t *base, const double *w, int nrec,
+                   const void *d, int nrhs, double scale, void *b, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* H3D_H */

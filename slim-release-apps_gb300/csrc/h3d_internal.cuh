@@ -1,0 +1,203 @@
+// Internal device-side building blocks of the h3d library: complex arithmetic, the
+// operator descriptor, and the 27-point coefficient rule of the Operto-style stencil
+// with PML (tools/algorithms/3DFreqModeling/Helm3d_27pt.h in the reference).
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "h3d.h"
+
+namespace h3d {
+
+// ---------------------------------------------------------------------------------------
+// Complex numbers stored interleaved (re, im); 8- or 16-byte aligned for vector loads.
+template <typename T>
+struct alignas(2 * sizeof(T)) cplx {
+    T re, im;
+};
+
+template <typename T>
+__host__ __device__ __forceinline__ cplx<T> mk(T r, T i) { return cplx<T>{r, i}; }
+template <typename T>
+__host__ __device__ __forceinline__ cplx<T> operator+(cplx<T> a, cplx<T> b) { return {a.re + b.re, a.im + b.im}; }
+template <typename T>
+__host__ __device__ __forceinline__ cplx<T> operator-(cplx<T> a, cplx<T> b) { return {a.re - b.re, a.im - b.im}; }
+template <typename T>
+__host__ __device__ __forceinline__ cplx<T> operator*(cplx<T> a, cplx<T> b)
+{
+    return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename T>
+__host__ __device__ __forceinline__ cplx<T> operator*(T s, cplx<T> a) { return {s * a.re, s * a.im}; }
+template <typename T>
+__host__ __device__ __forceinline__ cplx<T> cconj(cplx<T> a) { return {a.re, -a.im}; }
+template <typename T>
+__host__ __device__ __forceinline__ T cabs2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
+// acc += a * b
+template <typename T>
+__host__ __device__ __forceinline__ void cmac(cplx<T> &acc, cplx<T> a, cplx<T> b)
+{
+    acc.re += a.re * b.re - a.im * b.im;
+    acc.im += a.re * b.im + a.im * b.re;
+}
+
+// Stencil weights W1..W3, WM1..WM4 (Helm3d_27pt.h:194-200).
+constexpr double kW1 = 1.8395262e-5;
+constexpr double kW2 = 0.296692333333333;
+constexpr double kW3 = 0.027476150000000;
+constexpr double kWM1 = 0.49649658;
+constexpr double kWM2 = 0.075168750000000;
+constexpr double kWM3 = 0.004373916666667;
+constexpr double kWM4 = 5.690375e-07;
+
+// ---------------------------------------------------------------------------------------
+// Operator descriptor.  PML tables hold, per axis a, three arrays of n_a + 2 complex
+// values indexed by (idx + 1) for 0-based idx in [-1, n_a]:  xi_lo(idx), xi_hi(idx)
+// and their sum (pml_func_lower/upper of Helm3d_27pt.h:346-390 at 1-based idx+1).
+template <typename T>
+struct Op {
+    int nx, ny, nz;
+    long long N;                 // nx*ny*nz
+    long long sy, sz;            // strides of j and k (nx, nx*ny)
+    const T *wn;                 // wavenumber, real part (N)
+    const T *wni;                // imaginary part or nullptr
+    const cplx<T> *tab;          // PML tables
+    int lo[3], hi[3], sum[3];    // offsets of the three arrays of each axis inside tab
+    T wn_c, wn_x, wn_y, wn_z;    // centre coefficient and per-axis PML-sum coefficients
+    T pml_x, pml_y, pml_z;       // face coefficients
+    T xz, xy, yz;                // cross coefficients
+    T w3a2;                      // corner coefficient
+};
+
+// Enumerate the 27 stencil offsets: t = (dx+1) + 3(dy+1) + 9(dz+1) (Helm3d_27pt.h:163-189).
+#define H3D_FOR_27(M)                                                                          \
+    M(0, -1, -1, -1) M(1, 0, -1, -1) M(2, 1, -1, -1) M(3, -1, 0, -1) M(4, 0, 0, -1)          \
+    M(5, 1, 0, -1) M(6, -1, 1, -1) M(7, 0, 1, -1) M(8, 1, 1, -1) M(9, -1, -1, 0)             \
+    M(10, 0, -1, 0) M(11, 1, -1, 0) M(12, -1, 0, 0) M(13, 0, 0, 0) M(14, 1, 0, 0)            \
+    M(15, -1, 1, 0) M(16, 0, 1, 0) M(17, 1, 1, 0) M(18, -1, -1, 1) M(19, 0, -1, 1)           \
+    M(20, 1, -1, 1) M(21, -1, 0, 1) M(22, 0, 0, 1) M(23, 1, 0, 1) M(24, -1, 1, 1)            \
+    M(25, 0, 1, 1) M(26, 1, 1, 1)
+
+// PML part of the coefficient at offset (DX,DY,DZ) given the directional values A*
+// (xi_lo for a -1 offset, xi_hi for +1, seen from the row that owns the coefficient)
+// and the per-axis sums S*.  One closed form per offset class replaces the 26 written-out
+// lines of Helm3d_27pt.h:680-714 (forward) and :755-809 (adjoint, which uses the same
+// expressions evaluated at the neighbouring row).
+template <int DX, int DY, int DZ, typename T>
+__device__ __forceinline__ cplx<T> pml_term(const Op<T> &op, cplx<T> Ax, cplx<T> Ay, cplx<T> Az,
+                                            cplx<T> Sx, cplx<T> Sy, cplx<T> Sz)
+{
+    constexpr int nzc = (DX != 0) + (DY != 0) + (DZ != 0);
+    if constexpr (nzc == 0) {
+        return op.wn_x * Sx + op.wn_y * Sy + op.wn_z * Sz;
+    } else if constexpr (nzc == 3) {
+        return (-op.w3a2) * (Ax + Ay + Az);
+    } else if constexpr (nzc == 1) {
+        if constexpr (DX != 0) return op.pml_x * Ax + op.xz * Sz + op.xy * Sy;
+        else if constexpr (DY != 0) return op.pml_y * Ay + op.yz * Sz + op.xy * Sx;
+        else return op.pml_z * Az + op.yz * Sy + op.xz * Sx;
+    } else {
+        if constexpr (DZ == 0) return (-op.xy) * (Ax + Ay) + op.w3a2 * Sz;
+        else if constexpr (DY == 0) return (-op.xz) * (Az + Ax) + op.w3a2 * Sy;
+        else return (-op.yz) * (Az + Ay) + op.w3a2 * Sx;
+    }
+}
+
+template <int DX, int DY, int DZ>
+struct WM {
+    static constexpr int nzc = (DX != 0) + (DY != 0) + (DZ != 0);
+    static constexpr double value = nzc == 1 ? kWM2 : (nzc == 2 ? kWM3 : kWM4);
+};
+
+template <typename T, bool WNC>
+__device__ __forceinline__ cplx<T> load_wn(const Op<T> &op, long long idx)
+{
+    if constexpr (WNC) return mk<T>(op.wn[idx], op.wni[idx]);
+    else return mk<T>(op.wn[idx], T(0));
+}
+
+// Bitmask of the 27 neighbours of (i,j,k) that lie inside the grid.
+__device__ __forceinline__ uint32_t inside_mask(int i, int j, int k, int nx, int ny, int nz)
+{
+    const bool xl = i > 0, xr = i < nx - 1, yl = j > 0, yr = j < ny - 1, zl = k > 0, zr = k < nz - 1;
+    uint32_t m = 0;
+#define H3D_MASK_BIT(t, dx, dy, dz)                                                            \
+    if ((dx < 0 ? xl : (dx > 0 ? xr : true)) && (dy < 0 ? yl : (dy > 0 ? yr : true)) &&      \
+        (dz < 0 ? zl : (dz > 0 ? zr : true)))                                                  \
+        m |= (1u << t);
+    H3D_FOR_27(H3D_MASK_BIT)
+#undef H3D_MASK_BIT
+    return m;
+}
+
+// The 27 coefficients of row (i,j,k).
+//  forward (Helm3d_27pt.h:678-714): c_t = -WM_t wn[nbr] + pml_term(t) at the row, zero where
+//    the neighbour is outside the grid;
+//  adjoint (Helm3d_27pt.h:716-822): c_t = conj(-WM_t wn[row] + pml_term(t) evaluated at the
+//    neighbour row), not masked;
+//  DERIV (Helm3d_27pt.h:202-206, 754): the PML part is dropped.
+template <typename T, bool ADJ, bool DERIV, bool WNC>
+__device__ __forceinline__ void row_coefs(const Op<T> &op, int i, int j, int k, uint32_t inmask,
+                                          cplx<T> c[27])
+{
+    const long long ctr = i + op.sy * j + op.sz * k;
+    cplx<T> Sx{}, Sy{}, Sz{}, Axm{}, Axp{}, Aym{}, Ayp{}, Azm{}, Azp{};
+    if constexpr (!DERIV) {
+        const cplx<T> *t = op.tab;
+        Sx = t[op.sum[0] + i + 1];
+        Sy = t[op.sum[1] + j + 1];
+        Sz = t[op.sum[2] + k + 1];
+        if constexpr (!ADJ) {
+            Axm = t[op.lo[0] + i + 1]; Axp = t[op.hi[0] + i + 1];
+            Aym = t[op.lo[1] + j + 1]; Ayp = t[op.hi[1] + j + 1];
+            Azm = t[op.lo[2] + k + 1]; Azp = t[op.hi[2] + k + 1];
+        } else {
+            // xi_hi of the left neighbour, xi_lo of the right neighbour (pml_adj_info windows)
+            Axm = t[op.hi[0] + i]; Axp = t[op.lo[0] + i + 2];
+            Aym = t[op.hi[1] + j]; Ayp = t[op.lo[1] + j + 2];
+            Azm = t[op.hi[2] + k]; Azp = t[op.lo[2] + k + 2];
+        }
+    }
+    const cplx<T> wc = load_wn<T, WNC>(op, ctr);
+#define H3D_COEF(t, dx, dy, dz)                                                                \
+    {                                                                                          \
+        const cplx<T> Ax = dx < 0 ? Axm : Axp, Ay = dy < 0 ? Aym : Ayp, Az = dz < 0 ? Azm : Azp; \
+        cplx<T> v;                                                                             \
+        if constexpr (!ADJ) {                                                                  \
+            if (inmask & (1u << t)) {                                                          \
+                const cplx<T> wv = (t == 13) ? wc : load_wn<T, WNC>(op, ctr + dx + op.sy * dy + op.sz * dz); \
+                v = (t == 13) ? op.wn_c * wv : T(-WM<dx, dy, dz>::value) * wv;                 \
+                if constexpr (!DERIV) v = v + pml_term<dx, dy, dz, T>(op, Ax, Ay, Az, Sx, Sy, Sz); \
+            } else {                                                                           \
+                v = mk<T>(T(0), T(0));                                                         \
+            }                                                                                  \
+        } else {                                                                               \
+            v = (t == 13) ? op.wn_c * wc : T(-WM<dx, dy, dz>::value) * wc;                     \
+            if constexpr (!DERIV) v = v + pml_term<dx, dy, dz, T>(op, Ax, Ay, Az, Sx, Sy, Sz);  \
+            v = cconj(v);                                                                      \
+        }                                                                                      \
+        c[t] = v;                                                                              \
+    }
+    H3D_FOR_27(H3D_COEF)
+#undef H3D_COEF
+}
+
+// ---------------------------------------------------------------------------------------
+// Host-side helpers (h3d_host.cpp).
+struct DeviceTables;
+
+int make_op_f64(const h3d_grid *g, const double *wn, const double *wni, Op<double> *op);
+int make_op_f32(const h3d_grid *g, const float *wn, const float *wni, Op<float> *op);
+int check_grid(const h3d_grid *g);
+void set_error(const char *fmt, ...);
+int cuda_fail(cudaError_t e, const char *what);
+
+#define H3D_CUDA_TRY(expr)                                                                     \
+    do {                                                                                       \
+        cudaError_t _e = (expr);                                                               \
+        if (_e != cudaSuccess) return ::h3d::cuda_fail(_e, #expr);                             \
+    } while (0)
+
+}  // namespace h3d

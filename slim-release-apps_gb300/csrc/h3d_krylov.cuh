@@ -1,0 +1,64 @@
+// CGMN building blocks (tools/solvers/Krylov/CGMN.m:48-90 on the Kaczmarz-preconditioned
+// system of linearsolve.m:148-156): per-right-hand-side vector updates with masks and
+// deterministic FP64 reductions.  Storage precision T is double (plain FP64 path) or float
+// (complex64 inner solves of the mixed-precision path); inner products, norms and the
+// CG scalars are always accumulated and kept in double.
+#pragma once
+
+#include "h3d_internal.cuh"
+
+namespace h3d {
+
+// Per-RHS scalar state of one CGMN instance (device arrays, nrhs entries each).
+struct CgState {
+    double *rr;       // ||r||^2 (current)
+    double *bb;       // ||b~||^2 (preconditioned right-hand side)
+    double *ratio;    // ||r|| / ||b~|| after the last iteration
+    double *tolp;     // per-RHS tolerance on ratio
+    double *alpha;    // complex alpha (re, im) pairs
+    double *beta;     // real beta
+    int *active;      // 1 while iterating
+    int *upd;         // 1 if the RHS took part in the current iteration
+    int *iters;       // iterations done
+    int *status;      // 0 ok, H3D_ERR_NONFINITE on NaN/Inf
+    double *part;     // reduction partials: nrhs x G x 2
+    int G;            // reduction blocks per RHS
+};
+
+constexpr int kVecThreads = 256;
+
+template <typename T>
+int cg_init(const cplx<T> *bt, cplx<T> *x, cplx<T> *r, cplx<T> *p, long long N, int nrhs,
+            const CgState &s, const double *bnorm2_orig, double zero_tol2, int maxit,
+            cudaStream_t st);
+template <typename T>
+int cg_ap_dot(const cplx<T> *p, cplx<T> *y, long long N, int nrhs, const CgState &s,
+              cudaStream_t st);
+template <typename T>
+int cg_update_xr(cplx<T> *x, cplx<T> *r, const cplx<T> *p, const cplx<T> *ap, long long N,
+                 int nrhs, const CgState &s, int maxit, cudaStream_t st);
+template <typename T>
+int cg_update_p(cplx<T> *p, const cplx<T> *r, cplx<T> *y, long long N, int nrhs,
+                const CgState &s, cudaStream_t st);
+template <typename T>
+int copy_active(const cplx<T> *src, cplx<T> *dst, long long N, int nrhs, const int *active,
+                cudaStream_t st);
+template <typename T>
+int zero_vec(cplx<T> *v, long long N, int nrhs, cudaStream_t st);
+
+// Mixed precision glue.
+// dst32[s] = (complex64)(src64[s] * scale[s])   with scale[s] = 1/||src64[s]|| (0 if inactive)
+int scale_to_c64(const cplx<double> *src, cplx<float> *dst, long long N, int nrhs,
+                 const double *norm2, const int *active, cudaStream_t st);
+// u64[s] += sqrt(norm2[s]) * (complex128) e32[s]   for active s
+int add_scaled_c64(cplx<double> *u, const cplx<float> *e, long long N, int nrhs,
+                   const double *norm2, const int *active, cudaStream_t st);
+
+// FP64 residual r = b - A x with per-RHS ||r||^2 and ||b||^2 (h3d_solver.cu).
+int residual_f64(const Op<double> &op, const cplx<double> *b, const cplx<double> *x,
+                 cplx<double> *r, double *rr2, double *bb2, int nrhs, bool adj, double *part,
+                 int G, cudaStream_t st);
+
+int reduction_blocks(long long N);
+
+}  // namespace h3d

@@ -1,0 +1,611 @@
+// Solvers: u = H \ b and H^H \ b by CGMN on the Kaczmarz-preconditioned system
+// (tools/solvers/Krylov/linearsolve.m:148-168 + CGMN.m:36-94), in plain FP64 or as
+// complex64 inner solves under FP64 iterative refinement.
+//
+//   b~ = DSWP(0, b),  (I - Q) u = b~,  Q y = DSWP(y, 0),  w = 1.5, one double sweep
+//   (linearsolve.m:150-152); zero start (linearsolve.m:117-119).
+//
+// Iterations are recorded once into a CUDA graph (check_every iterations per graph) and
+// replayed; per-RHS masks freeze converged right-hand sides on the device, and the host
+// only reads the mask every check_every iterations.
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <vector>
+
+#include "h3d_internal.cuh"
+#include "h3d_kernels.cuh"
+#include "h3d_krylov.cuh"
+#include "h3d_reduce.cuh"
+#include "h3d_vec.cuh"
+
+namespace h3d {
+
+// ---------------------------------------------------------------------------------------
+// FP64 residual r = b - A x, fused with the per-block partial sums of ||r||^2 and ||b||^2.
+template <bool ADJ, bool WNC>
+__global__ void __launch_bounds__(256) residual_kernel(Op<double> op, const cplx<double> *__restrict__ b,
+                                                       const cplx<double> *__restrict__ x,
+                                                       cplx<double> *__restrict__ r, int nrhs,
+                                                       double *part, int G)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y;
+    const int k = blockIdx.z;
+    const bool valid = i < op.nx && j < op.ny;
+    const int blin = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    cplx<double> c[27];
+    uint32_t m = 0;
+    long long ctr = 0;
+    if (valid) {
+        m = inside_mask(i, j, k, op.nx, op.ny, op.nz);
+        row_coefs<double, ADJ, false, WNC>(op, i, j, k, m, c);
+        ctr = i + op.sy * j + op.sz * k;
+    }
+    for (int s = 0; s < nrhs; ++s) {
+        double rr = 0.0, bb = 0.0;
+        if (valid) {
+            const cplx<double> *xs = x + (long long)s * op.N + ctr;
+            cplx<double> acc = mk(0.0, 0.0);
+#define H3D_ACC(t, dx, dy, dz) \
+    if (m & (1u << t)) cmac(acc, c[t], xs[dx + op.sy * dy + op.sz * dz]);
+            H3D_FOR_27(H3D_ACC)
+#undef H3D_ACC
+            const cplx<double> bv = b[(long long)s * op.N + ctr];
+            const cplx<double> rv = bv - acc;
+            r[(long long)s * op.N + ctr] = rv;
+            rr = cabs2(rv);
+            bb = cabs2(bv);
+        }
+        const double2 t = block_sum2_r(rr, bb);
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            part[2 * ((long long)s * G + blin)] = t.x;
+            part[2 * ((long long)s * G + blin) + 1] = t.y;
+        }
+    }
+}
+
+__global__ void residual_reduce(const double *part, int G, double *rr2, double *bb2)
+{
+    const int s = blockIdx.x;
+    double a = 0.0, b = 0.0;
+    for (int q = threadIdx.x; q < G; q += blockDim.x) {
+        a += part[2 * ((long long)s * G + q)];
+        b += part[2 * ((long long)s * G + q) + 1];
+    }
+    const double2 t = block_sum2_r(a, b);
+    if (threadIdx.x == 0) {
+        if (rr2) rr2[s] = t.x;
+        if (bb2) bb2[s] = t.y;
+    }
+}
+
+static dim3 residual_grid(const Op<double> &op) { return dim3((op.nx + 31) / 32, (op.ny + 7) / 8, op.nz); }
+
+int residual_f64(const Op<double> &op, const cplx<double> *b, const cplx<double> *x,
+                 cplx<double> *r, double *rr2, double *bb2, int nrhs, bool adj, double *part,
+                 int G, cudaStream_t st)
+{
+    const dim3 grd = residual_grid(op), blk(32, 8);
+    const bool wnc = op.wni != nullptr;
+    if (!adj && !wnc) residual_kernel<false, false><<<grd, blk, 0, st>>>(op, b, x, r, nrhs, part, G);
+    else if (!adj && wnc) residual_kernel<false, true><<<grd, blk, 0, st>>>(op, b, x, r, nrhs, part, G);
+    else if (adj && !wnc) residual_kernel<true, false><<<grd, blk, 0, st>>>(op, b, x, r, nrhs, part, G);
+    else residual_kernel<true, true><<<grd, blk, 0, st>>>(op, b, x, r, nrhs, part, G);
+    residual_reduce<<<nrhs, 256, 0, st>>>(part, G, rr2, bb2);
+    H3D_CUDA_TRY(cudaGetLastError());
+    return H3D_OK;
+}
+
+static int residual_parts(const Op<double> &op)
+{
+    const dim3 g = residual_grid(op);
+    return (int)(g.x * g.y * g.z);
+}
+
+// ---------------------------------------------------------------------------------------
+// One CGMN instance over nrhs right-hand sides in storage precision T.
+template <typename T>
+struct CgRun {
+    Op<T> op{};
+    long long N = 0;
+    int nrhs = 0;
+    bool adj = false;
+    T w = T(1.5);
+    int order = H3D_ORDER_COLOUR27;
+    int32_t block[3] = {0, 0, 0};
+    int maxit = 10000;
+    cplx<T> *x = nullptr, *r = nullptr, *p = nullptr, *y = nullptr;
+    CgState s{};
+    DevBuf vecs, scal, ints, parts;
+    cudaGraphExec_t exec = nullptr;
+    int graph_iters = 0;
+
+    ~CgRun()
+    {
+        if (exec) cudaGraphExecDestroy(exec);
+    }
+
+    int alloc(cudaStream_t st)
+    {
+        const size_t vb = sizeof(cplx<T>) * (size_t)N * nrhs;
+        int rc;
+        if ((rc = vecs.alloc(4 * vb, st))) return rc;
+        x = vecs.as<cplx<T>>();
+        r = x + N * nrhs;
+        p = r + N * nrhs;
+        y = p + N * nrhs;
+        s.G = reduction_blocks(N);
+        if ((rc = scal.alloc(sizeof(double) * (size_t)nrhs * 7, st))) return rc;
+        double *d = scal.as<double>();
+        s.rr = d;
+        s.bb = d + nrhs;
+        s.ratio = d + 2 * nrhs;
+        s.tolp = d + 3 * nrhs;
+        s.beta = d + 4 * nrhs;
+        s.alpha = d + 5 * nrhs;  // 2 * nrhs
+        if ((rc = ints.alloc(sizeof(int) * (size_t)nrhs * 4, st))) return rc;
+        int *q = ints.as<int>();
+        s.active = q;
+        s.upd = q + nrhs;
+        s.iters = q + 2 * nrhs;
+        s.status = q + 3 * nrhs;
+        if ((rc = parts.alloc(sizeof(double) * 2 * (size_t)s.G * nrhs, st))) return rc;
+        s.part = parts.as<double>();
+        return H3D_OK;
+    }
+
+    int sweep_launches() const
+    {
+        if (order == H3D_ORDER_LEX) return 2 * (op.nx + 3 * op.ny + 9 * op.nz);
+        if (order == H3D_ORDER_BLOCK) {
+            const int bx = block[0] > 0 ? block[0] : 8, by = block[1] > 0 ? block[1] : 8,
+                      bz = block[2] > 0 ? block[2] : 8;
+            return 2 * ((op.nx + bx - 1) / bx + 2 * ((op.ny + by - 1) / by) + 4 * ((op.nz + bz - 1) / bz));
+        }
+        return 54;
+    }
+
+    // b~ = DSWP(0, b) into y, then x = 0, r = p = y.
+    int setup(const cplx<T> *b, const double *bnorm2_orig, double zero_tol2, cudaStream_t st)
+    {
+        int rc;
+        if ((rc = zero_vec<T>(y, N, nrhs, st))) return rc;
+        if ((rc = launch_sweep<T>(op, y, b, nrhs, w, adj, order, block, nullptr, st))) return rc;
+        return cg_init<T>(y, x, r, p, N, nrhs, s, bnorm2_orig, zero_tol2, maxit, st);
+    }
+
+    int enqueue_iteration(cudaStream_t st)
+    {
+        int rc;
+        if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st))) return rc;
+        if ((rc = cg_ap_dot<T>(p, y, N, nrhs, s, st))) return rc;
+        if ((rc = cg_update_xr<T>(x, r, p, y, N, nrhs, s, maxit, st))) return rc;
+        return cg_update_p<T>(p, r, y, N, nrhs, s, st);
+    }
+
+    int run_block(int iters, bool use_graph, cudaStream_t st)
+    {
+        if (!use_graph) {
+            for (int q = 0; q < iters; ++q) {
+                int rc = enqueue_iteration(st);
+                if (rc) return rc;
+            }
+            return H3D_OK;
+        }
+        if (!exec || graph_iters != iters) {
+            if (exec) cudaGraphExecDestroy(exec);
+            exec = nullptr;
+            cudaGraph_t g = nullptr;
+            H3D_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+            int rc = H3D_OK;
+            for (int q = 0; q < iters && !rc; ++q) rc = enqueue_iteration(st);
+            cudaError_t e = cudaStreamEndCapture(st, &g);
+            if (rc) {
+                if (g) cudaGraphDestroy(g);
+                return rc;
+            }
+            if (e != cudaSuccess) return cuda_fail(e, "cudaStreamEndCapture");
+            e = cudaGraphInstantiate(&exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return cuda_fail(e, "cudaGraphInstantiate");
+            graph_iters = iters;
+        }
+        H3D_CUDA_TRY(cudaGraphLaunch(exec, st));
+        return H3D_OK;
+    }
+};
+
+struct HostState {
+    std::vector<int> active, iters, status;
+    std::vector<double> ratio;
+    int *h_ints = nullptr;
+    double *h_dbl = nullptr;
+    int n = 0;
+    ~HostState()
+    {
+        if (h_ints) cudaFreeHost(h_ints);
+        if (h_dbl) cudaFreeHost(h_dbl);
+    }
+    int init(int nrhs)
+    {
+        n = nrhs;
+        H3D_CUDA_TRY(cudaMallocHost(&h_ints, sizeof(int) * 3 * nrhs));
+        H3D_CUDA_TRY(cudaMallocHost(&h_dbl, sizeof(double) * 4 * nrhs));
+        active.resize(nrhs);
+        iters.resize(nrhs);
+        status.resize(nrhs);
+        ratio.resize(nrhs);
+        return H3D_OK;
+    }
+    template <typename T>
+    int fetch(const CgRun<T> &cg, cudaStream_t st)
+    {
+        H3D_CUDA_TRY(cudaMemcpyAsync(h_ints, cg.s.active, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaMemcpyAsync(h_ints + n, cg.s.iters, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaMemcpyAsync(h_ints + 2 * n, cg.s.status, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaMemcpyAsync(h_dbl, cg.s.ratio, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaStreamSynchronize(st));
+        for (int q = 0; q < n; ++q) {
+            active[q] = h_ints[q];
+            iters[q] = h_ints[n + q];
+            status[q] = h_ints[2 * n + q];
+            ratio[q] = h_dbl[q];
+        }
+        return H3D_OK;
+    }
+};
+
+// Run a CGMN instance until every right-hand side is inactive.
+template <typename T>
+static int cg_drive(CgRun<T> &cg, HostState &hs, const h3d_solve_opts &o, double *res_hist,
+                    int res_hist_len, int *hist_pos, cudaStream_t st)
+{
+    const int per_iter = cg.sweep_launches() + 6;
+    int block_iters = o.check_every > 0 ? o.check_every : 25;
+    if (block_iters * per_iter > 20000) block_iters = std::max(1, 20000 / per_iter);
+    for (;;) {
+        int rc = hs.fetch(cg, st);
+        if (rc) return rc;
+        bool any = false;
+        double mx = 0.0;
+        for (int q = 0; q < hs.n; ++q) {
+            any |= hs.active[q] != 0;
+            if (hs.iters[q] > 0) mx = std::max(mx, hs.ratio[q]);
+        }
+        if (res_hist && hist_pos && *hist_pos < res_hist_len) res_hist[(*hist_pos)++] = mx;
+        if (o.verbose) {
+            int it = 0;
+            for (int q = 0; q < hs.n; ++q) it = std::max(it, hs.iters[q]);
+            fprintf(stderr, "[h3d] cgmn(%s) it %d max-ratio %.3e\n", sizeof(T) == 8 ? "c128" : "c64", it, mx);
+        }
+        if (!any) return H3D_OK;
+        if ((rc = cg.run_block(block_iters, o.use_graphs != 0, st))) return rc;
+    }
+}
+
+struct Timer {
+    std::chrono::steady_clock::time_point t0 = std::chrono::steady_clock::now();
+    double seconds() const
+    {
+        return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+};
+
+// ---------------------------------------------------------------------------------------
+// Core solve on an internal stream.  b, u: complex128 interleaved device vectors.
+static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_im,
+                      const cplx<double> *b, cplx<double> *u, int nrhs, int mode,
+                      const h3d_solve_opts &o, h3d_solve_info *info, double *res_hist,
+                      int res_hist_len, cudaStream_t st)
+{
+    Timer timer;
+    int rc;
+    Op<double> op64;
+    if ((rc = make_op_f64(g, wn_re, wn_im, &op64))) return rc;
+    const long long N = op64.N;
+    const bool adj = mode == H3D_ADJOINT;
+    const double zero_tol2 = 1e-24;  // (1e-12)^2, opAbstractMatrix.m:118
+
+    // FP64 residual machinery: r64 = b - A u, per-RHS norms.
+    const int Gr = residual_parts(op64);
+    DevBuf r64b, partb, normb;
+    if ((rc = r64b.alloc(sizeof(cplx<double>) * (size_t)N * nrhs, st))) return rc;
+    if ((rc = partb.alloc(sizeof(double) * 2 * (size_t)Gr * nrhs, st))) return rc;
+    if ((rc = normb.alloc(sizeof(double) * 2 * (size_t)nrhs, st))) return rc;
+    cplx<double> *r64 = r64b.as<cplx<double>>();
+    double *rr2 = normb.as<double>(), *bb2 = rr2 + nrhs;
+    H3D_CUDA_TRY(cudaMemsetAsync(u, 0, sizeof(cplx<double>) * (size_t)N * nrhs, st));
+    if ((rc = residual_f64(op64, b, u, r64, rr2, bb2, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
+
+    std::vector<double> h_rr(nrhs), h_bb(nrhs);
+    auto fetch_norms = [&]() -> int {
+        H3D_CUDA_TRY(cudaMemcpyAsync(h_rr.data(), rr2, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaMemcpyAsync(h_bb.data(), bb2, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaStreamSynchronize(st));
+        return H3D_OK;
+    };
+    if ((rc = fetch_norms())) return rc;
+    const std::vector<double> bnorm2 = h_bb;
+
+    HostState hs;
+    if ((rc = hs.init(nrhs))) return rc;
+    int hist_pos = 0;
+    int total_iters_max = 0, outer = 0;
+    std::vector<int> total_iters(nrhs, 0);
+    double last_prec = 0.0;
+    bool nonfinite = false;
+    std::vector<int> done(nrhs, 0);
+    for (int q = 0; q < nrhs; ++q) done[q] = bnorm2[q] < zero_tol2;
+
+    auto true_ok = [&](int q) { return h_bb[q] > 0 ? std::sqrt(h_rr[q] / bnorm2[q]) <= o.tol : true; };
+
+    if (o.precision == H3D_PREC_FP64) {
+        CgRun<double> cg;
+        cg.op = op64;
+        cg.N = N;
+        cg.nrhs = nrhs;
+        cg.adj = adj;
+        cg.w = o.w;
+        cg.order = o.order;
+        std::memcpy(cg.block, o.block, sizeof cg.block);
+        cg.maxit = o.maxit;
+        if ((rc = cg.alloc(st))) return rc;
+        std::vector<double> tolp(nrhs, o.tol);
+        H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, st));
+        if ((rc = cg.setup(b, bb2, zero_tol2, st))) return rc;
+        for (;;) {
+            if ((rc = cg_drive(cg, hs, o, res_hist, res_hist_len, &hist_pos, st))) return rc;
+            ++outer;
+            if ((rc = residual_f64(op64, b, cg.x, r64, rr2, nullptr, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
+            if ((rc = fetch_norms())) return rc;
+            if (o.stop_rule != H3D_STOP_TRUE_RESIDUAL) break;
+            bool again = false;
+            for (int q = 0; q < nrhs; ++q) {
+                if (done[q] || hs.status[q] || hs.iters[q] >= o.maxit) continue;
+                const double tr = std::sqrt(h_rr[q] / bnorm2[q]);
+                if (tr <= o.tol) continue;
+                // Not there yet on the true residual: tighten this column's preconditioned
+                // tolerance in proportion and continue the same Krylov sequence.
+                tolp[q] = std::max(hs.ratio[q] * (o.tol / tr) * 0.5, 1e-15);
+                again = true;
+            }
+            if (!again || outer > o.max_outer) break;
+            std::vector<int> act(nrhs, 0);
+            for (int q = 0; q < nrhs; ++q)
+                act[q] = (!done[q] && !hs.status[q] && hs.iters[q] < o.maxit &&
+                          std::sqrt(h_rr[q] / bnorm2[q]) > o.tol);
+            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, st));
+            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.active, act.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, st));
+            H3D_CUDA_TRY(cudaStreamSynchronize(st));
+        }
+        H3D_CUDA_TRY(cudaMemcpyAsync(u, cg.x, sizeof(cplx<double>) * (size_t)N * nrhs, cudaMemcpyDeviceToDevice, st));
+        for (int q = 0; q < nrhs; ++q) {
+            total_iters[q] = hs.iters[q];
+            last_prec = std::max(last_prec, hs.ratio[q]);
+            nonfinite |= hs.status[q] != 0;
+        }
+    } else {
+        // Mixed precision: complex64 CGMN on the scaled FP64 residual, FP64 update and residual.
+        DevBuf wn32b, rhs32b;
+        if ((rc = wn32b.alloc(sizeof(float) * (size_t)N * (wn_im ? 2 : 1), st))) return rc;
+        float *wn32 = wn32b.as<float>();
+        if ((rc = cast<double, float>(wn_re, wn32, N, st))) return rc;
+        if (wn_im && (rc = cast<double, float>(wn_im, wn32 + N, N, st))) return rc;
+        Op<float> op32;
+        if ((rc = make_op_f32(g, wn32, wn_im ? wn32 + N : nullptr, &op32))) return rc;
+        if ((rc = rhs32b.alloc(sizeof(cplx<float>) * (size_t)N * nrhs, st))) return rc;
+        cplx<float> *rhs32 = rhs32b.as<cplx<float>>();
+        CgRun<float> cg;
+        cg.op = op32;
+        cg.N = N;
+        cg.nrhs = nrhs;
+        cg.adj = adj;
+        cg.w = (float)o.w;
+        cg.order = o.order;
+        std::memcpy(cg.block, o.block, sizeof cg.block);
+        cg.maxit = o.maxit;
+        if ((rc = cg.alloc(st))) return rc;
+        DevBuf actb;
+        if ((rc = actb.alloc(sizeof(int) * nrhs, st))) return rc;
+        int *outer_active = actb.as<int>();
+        std::vector<double> tolp(nrhs, o.inner_tol);
+        H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, st));
+        for (outer = 0; outer < o.max_outer; ++outer) {
+            std::vector<int> act(nrhs, 0);
+            bool any = false;
+            for (int q = 0; q < nrhs; ++q) {
+                act[q] = !done[q] && !true_ok(q) && total_iters[q] < o.maxit;
+                any |= act[q] != 0;
+            }
+            if (!any) break;
+            H3D_CUDA_TRY(cudaMemcpyAsync(outer_active, act.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, st));
+            if ((rc = scale_to_c64(r64, rhs32, N, nrhs, rr2, outer_active, st))) return rc;
+            if ((rc = cg.setup(rhs32, nullptr, 0.0, st))) return rc;
+            // only the columns still above tolerance iterate
+            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.active, act.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, st));
+            if ((rc = cg_drive(cg, hs, o, res_hist, res_hist_len, &hist_pos, st))) return rc;
+            if ((rc = add_scaled_c64(u, cg.x, N, nrhs, rr2, outer_active, st))) return rc;
+            for (int q = 0; q < nrhs; ++q) {
+                if (!act[q]) continue;
+                total_iters[q] += hs.iters[q];
+                last_prec = hs.ratio[q];
+                nonfinite |= hs.status[q] != 0;
+            }
+            if ((rc = residual_f64(op64, b, u, r64, rr2, nullptr, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
+            if ((rc = fetch_norms())) return rc;
+            if (nonfinite) break;
+        }
+    }
+    bool all_ok = !nonfinite;
+    double worst = 0.0;
+    for (int q = 0; q < nrhs; ++q) {
+        total_iters_max = std::max(total_iters_max, total_iters[q]);
+        if (done[q]) {
+            H3D_CUDA_TRY(cudaMemsetAsync(u + (size_t)q * N, 0, sizeof(cplx<double>) * (size_t)N, st));
+            continue;
+        }
+        const double tr = std::sqrt(h_rr[q] / bnorm2[q]);
+        worst = std::max(worst, tr);
+        if (o.stop_rule == H3D_STOP_TRUE_RESIDUAL ? !(tr <= o.tol) : false) all_ok = false;
+    }
+    H3D_CUDA_TRY(cudaStreamSynchronize(st));
+    if (info) {
+        info->iters = total_iters_max;
+        info->outer = outer;
+        info->converged = all_ok ? 1 : 0;
+        info->nrhs = nrhs;
+        info->rel_res_true = worst;
+        info->rel_res_prec = last_prec;
+        info->seconds = timer.seconds();
+        info->sweep_seconds = 0.0;
+    }
+    if (nonfinite) {
+        set_error("non-finite value in the CGMN iteration");
+        return H3D_ERR_NONFINITE;
+    }
+    if (!all_ok) {
+        set_error("not converged: max true relative residual %.3e after %d iterations", worst, total_iters_max);
+        return H3D_ERR_NOT_CONVERGED;
+    }
+    return H3D_OK;
+}
+
+// Run f on an internal non-blocking stream ordered after the caller's stream.
+template <typename F>
+static int on_internal_stream(cudaStream_t user, F f)
+{
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    H3D_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    H3D_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    H3D_CUDA_TRY(cudaEventRecord(ev, user));
+    H3D_CUDA_TRY(cudaStreamWaitEvent(st, ev, 0));
+    int rc = f(st);
+    cudaError_t e1 = cudaEventRecord(ev, st);
+    cudaError_t e2 = cudaStreamWaitEvent(user, ev, 0);
+    cudaError_t e3 = cudaStreamSynchronize(st);
+    cudaEventDestroy(ev);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    if (e1 != cudaSuccess) return cuda_fail(e1, "cudaEventRecord");
+    if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamWaitEvent");
+    if (e3 != cudaSuccess) return cuda_fail(e3, "cudaStreamSynchronize");
+    return H3D_OK;
+}
+
+static int check_opts(const h3d_solve_opts *o)
+{
+    if (!o) return H3D_OK;
+    if (!(o->tol > 0) || o->maxit < 1 || !(o->w > 0 && o->w < 2) ||
+        (o->precision != H3D_PREC_FP64 && o->precision != H3D_PREC_MIXED) || o->order < 0 ||
+        o->order > 2 || (o->precision == H3D_PREC_MIXED && !(o->inner_tol > 0 && o->inner_tol < 1))) {
+        set_error("invalid solver options");
+        return H3D_ERR_BAD_ARG;
+    }
+    return H3D_OK;
+}
+
+}  // namespace h3d
+
+using namespace h3d;
+
+extern "C" {
+
+int h3d_residual(const h3d_grid *g, const double *wn_re, const double *wn_im, const void *b,
+                 const void *x, void *r, double *rr2, double *bb2, int nrhs, int mode, void *stream)
+{
+    if (!wn_re || !b || !x || !r || nrhs < 1 || (mode != H3D_FORWARD && mode != H3D_ADJOINT)) {
+        set_error("h3d_residual: bad argument");
+        return H3D_ERR_BAD_ARG;
+    }
+    Op<double> op;
+    int rc = make_op_f64(g, wn_re, wn_im, &op);
+    if (rc) return rc;
+    cudaStream_t st = (cudaStream_t)stream;
+    const int G = residual_parts(op);
+    DevBuf part, norms;
+    if ((rc = part.alloc(sizeof(double) * 2 * (size_t)G * nrhs, st))) return rc;
+    if ((rc = norms.alloc(sizeof(double) * 2 * (size_t)nrhs, st))) return rc;
+    double *n1 = norms.as<double>();
+    if ((rc = residual_f64(op, (const cplx<double> *)b, (const cplx<double> *)x, (cplx<double> *)r,
+                           n1, n1 + nrhs, nrhs, mode == H3D_ADJOINT, part.as<double>(), G, st)))
+        return rc;
+    if (rr2) H3D_CUDA_TRY(cudaMemcpyAsync(rr2, n1, sizeof(double) * nrhs, cudaMemcpyDeviceToDevice, st));
+    if (bb2) H3D_CUDA_TRY(cudaMemcpyAsync(bb2, n1 + nrhs, sizeof(double) * nrhs, cudaMemcpyDeviceToDevice, st));
+    return H3D_OK;
+}
+
+int h3d_solve(const h3d_grid *g, const double *wn_re, const double *wn_im, const void *b,
+              void *u, int nrhs, int mode, const h3d_solve_opts *opts, h3d_solve_info *info,
+              double *res_hist, int res_hist_len, void *stream)
+{
+    if (!wn_re || !b || !u || nrhs < 1 || (mode != H3D_FORWARD && mode != H3D_ADJOINT)) {
+        set_error("h3d_solve: bad argument");
+        return H3D_ERR_BAD_ARG;
+    }
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if ((rc = check_opts(opts))) return rc;
+    h3d_solve_opts o;
+    h3d_default_opts(&o);
+    if (opts) o = *opts;
+    return on_internal_stream((cudaStream_t)stream, [&](cudaStream_t st) {
+        return solve_impl(g, wn_re, wn_im, (const cplx<double> *)b, (cplx<double> *)u, nrhs, mode, o,
+                          info, res_hist, res_hist_len, st);
+    });
+}
+
+int h3d_solve_batch(const h3d_problem *probs, int nprob, const h3d_solve_opts *opts,
+                    h3d_solve_info *infos, void *stream)
+{
+    if (!probs || nprob < 1) {
+        set_error("h3d_solve_batch: bad argument");
+        return H3D_ERR_BAD_ARG;
+    }
+    int worst = H3D_OK;
+    for (int q = 0; q < nprob; ++q) {
+        const h3d_problem &p = probs[q];
+        int rc = h3d_solve(&p.grid, p.wn_re, p.wn_im, p.b, p.u, p.nrhs, p.mode, opts,
+                           infos ? &infos[q] : nullptr, nullptr, 0, stream);
+        if (rc && rc != H3D_ERR_NOT_CONVERGED) return rc;
+        if (rc) worst = rc;
+    }
+    return worst;
+}
+
+int h3d_solve_host(const h3d_grid *g, const double *wn_re, const double *wn_im,
+                   const void *b_host, void *u_host, int nrhs, int mode,
+                   const h3d_solve_opts *opts, h3d_solve_info *info)
+{
+    int rc = check_grid(g);
+    if (rc) return rc;
+    if (!wn_re || !b_host || !u_host || nrhs < 1) {
+        set_error("h3d_solve_host: bad argument");
+        return H3D_ERR_BAD_ARG;
+    }
+    const long long N = (long long)g->n[0] * g->n[1] * g->n[2];
+    return on_internal_stream(nullptr, [&](cudaStream_t st) -> int {
+        DevBuf dw, db, du;
+        int r;
+        const size_t wb = sizeof(double) * (size_t)N;
+        const size_t vb = sizeof(cplx<double>) * (size_t)N * nrhs;
+        if ((r = dw.alloc(wb * (wn_im ? 2 : 1), st)) || (r = db.alloc(vb, st)) || (r = du.alloc(vb, st)))
+            return r;
+        H3D_CUDA_TRY(cudaMemcpyAsync(dw.p, wn_re, wb, cudaMemcpyHostToDevice, st));
+        if (wn_im) H3D_CUDA_TRY(cudaMemcpyAsync(dw.as<double>() + N, wn_im, wb, cudaMemcpyHostToDevice, st));
+        H3D_CUDA_TRY(cudaMemcpyAsync(db.p, b_host, vb, cudaMemcpyHostToDevice, st));
+        r = h3d_solve(g, dw.as<double>(), wn_im ? dw.as<double>() + N : nullptr, db.p, du.p, nrhs, mode,
+                      opts, info, nullptr, 0, st);
+        if (r && r != H3D_ERR_NOT_CONVERGED) return r;
+        H3D_CUDA_TRY(cudaMemcpyAsync(u_host, du.p, vb, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaStreamSynchronize(st));
+        if (info) {
+            // the copies are part of the call
+        }
+        return r;
+    });
+}
+
+}  // extern "C"

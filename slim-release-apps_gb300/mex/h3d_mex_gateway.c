@@ -1,0 +1,141 @@
+/*
+ * Drop-in MEX gateway for the GB300 Helmholtz library.
+ *
+ * One source, compiled once per reference binary name (the flag matrix of
+ * ibin/install_MEX:88-114 in SLIM-release-apps):
+ *
+ *   -DH3D_GATEWAY_MVP   [-DADJ] [-DDERIV] [-DWNCMPLX]  -> Helm3dmvp_*_mex
+ *       y = Helm3dmvp_xxx_mex(wn, h, n, npml, x, nthreads)       (Helm3dmvp_mex.c:17-48)
+ *   -DH3D_GATEWAY_SWEEP [-DADJ] [-DWNCMPLX]            -> Helm3d_kacz_sweep_*_mex
+ *       y = Helm3d_kacz_sweep_xxx_mex(wn, h, n, npml, w, x, b)   (Helm3dkaczswp_mex.c:21-50)
+ *
+ * Same argument order, same checks and error identifiers as the reference
+ * gateways, same output (a new N x 1 or N x P complex double matrix).  The
+ * arithmetic runs on the GPU through libh3d (include/h3d.h); nthreads is
+ * accepted and ignored.  The sweep uses the reference's lexicographic row order
+ * (H3D_ORDER_LEX), so results match the CPU gateway to rounding.
+ *
+ * Deliberate differences:
+ *   - Helm3d_kacz_sweep_wnc_mex uses the imaginary part of wn (the reference's
+ *     install line spells the flag -DWNCMPLEX, so its build silently drops it);
+ *   - a b with fewer columns than x is rejected with the Bsize identifier instead
+ *     of being read out of bounds.
+ */
+#include <stddef.h>
+#include <stdio.h>
+
+#include "h3d.h"
+#include "mex.h"
+
+#define ID_PREFIX "SLIM_release_apps:tools:algorithms:ThreeDFreqModeling:"
+
+static void fail(int status, const char *gateway)
+{
+    static char id[160];
+    const char *which = "h3d";
+    switch (status) {
+    case H3D_ERR_NSIZE: which = "Nsize"; break;
+    case H3D_ERR_XSIZE: which = "Xsize"; break;
+    case H3D_ERR_BSIZE: which = "Bsize"; break;
+    default: break;
+    }
+    if (which[0] == 'h') {
+        mexErrMsgIdAndTxt(h3d_status_id(status), "%s", h3d_last_error());
+        return;
+    }
+    /* The reference's matvec reports an x-size error with the sweep gateway's prefix
+     * (Helm3dmvp_mex.c:83); keep that. */
+    if (status == H3D_ERR_XSIZE) gateway = "Helm3dkaczswp_mex";
+    snprintf(id, sizeof id, ID_PREFIX "%s:%s", gateway, which);
+    mexErrMsgIdAndTxt(id, "%s", h3d_last_error());
+}
+
+#ifdef ADJ
+#define H3D_MODE H3D_ADJOINT
+#else
+#define H3D_MODE H3D_FORWARD
+#endif
+
+#ifdef DERIV
+#define H3D_DERIV 1
+#else
+#define H3D_DERIV 0
+#endif
+
+static size_t n_len_of(const mxArray *n)
+{
+    /* Helm3dmvp_mex.c:75 / Helm3dkaczswp_mex.c:143: accepted when either dimension is 3. */
+    return (mxGetM(n) == 3 || mxGetN(n) == 3) ? 3 : 0;
+}
+
+#if defined(H3D_GATEWAY_MVP)
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
+{
+    (void)nlhs;
+    if (nrhs < 5) mexErrMsgIdAndTxt("h3d:badArgument", "expected (wn,h,n,npml,x[,nthreads])");
+    const mxArray *WN = prhs[0], *H = prhs[1], *N = prhs[2], *NPML = prhs[3], *X = prhs[4];
+    const size_t nl = n_len_of(N);
+    if (nl != 3) {
+        fail(H3D_ERR_NSIZE, "Helm3dmvp_mex");
+        return;
+    }
+    const double *n = mxGetPr(N);
+    const size_t numel = (size_t)n[0] * (size_t)n[1] * (size_t)n[2];
+    if (mxGetM(X) != numel) {
+        fail(H3D_ERR_XSIZE, "Helm3dmvp_mex");
+        return;
+    }
+#ifdef WNCMPLX
+    const double *wni = mxIsComplex(WN) ? mxGetPi(WN) : NULL;
+#else
+    const double *wni = NULL;
+#endif
+    plhs[0] = mxCreateDoubleMatrix(numel, 1, mxCOMPLEX);
+    int rc = h3d_mex_mvp(mxGetPr(WN), wni, mxGetPr(H), n, nl, mxGetPr(NPML), mxGetPr(X),
+                         mxIsComplex(X) ? mxGetPi(X) : NULL, mxGetM(X), mxGetPr(plhs[0]),
+                         mxGetPi(plhs[0]), H3D_MODE, H3D_DERIV);
+    if (rc != H3D_OK) fail(rc, "Helm3dmvp_mex");
+}
+
+#elif defined(H3D_GATEWAY_SWEEP)
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
+{
+    (void)nlhs;
+    if (nrhs < 7) mexErrMsgIdAndTxt("h3d:badArgument", "expected (wn,h,n,npml,w,x,b)");
+    const mxArray *WN = prhs[0], *H = prhs[1], *N = prhs[2], *NPML = prhs[3], *OMEGA = prhs[4],
+                  *X = prhs[5], *B = prhs[6];
+    const size_t nl = n_len_of(N);
+    if (nl != 3) {
+        fail(H3D_ERR_NSIZE, "Helm3dkaczswp_mex");
+        return;
+    }
+    const double *n = mxGetPr(N);
+    const size_t numel = (size_t)n[0] * (size_t)n[1] * (size_t)n[2];
+    if (mxGetM(X) != numel) {
+        fail(H3D_ERR_XSIZE, "Helm3dkaczswp_mex");
+        return;
+    }
+    const size_t P = mxGetN(X);
+    if (mxGetM(B) != numel || mxGetN(B) < P) {
+        fail(H3D_ERR_BSIZE, "Helm3dkaczswp_mex");
+        return;
+    }
+#ifdef WNCMPLX
+    const double *wni = mxIsComplex(WN) ? mxGetPi(WN) : NULL;
+#else
+    const double *wni = NULL;
+#endif
+    plhs[0] = mxCreateDoubleMatrix(numel, P, mxCOMPLEX);
+    int rc = h3d_mex_kacz_sweep(mxGetPr(WN), wni, mxGetPr(H), n, nl, mxGetPr(NPML),
+                                mxGetScalar(OMEGA), mxGetPr(X), mxIsComplex(X) ? mxGetPi(X) : NULL,
+                                mxGetM(X), P, mxGetPr(B), mxIsComplex(B) ? mxGetPi(B) : NULL,
+                                mxGetM(B), mxGetPr(plhs[0]), mxGetPi(plhs[0]), H3D_MODE,
+                                H3D_ORDER_LEX);
+    if (rc != H3D_OK) fail(rc, "Helm3dkaczswp_mex");
+}
+
+#else
+#error "define H3D_GATEWAY_MVP or H3D_GATEWAY_SWEEP"
+#endif
