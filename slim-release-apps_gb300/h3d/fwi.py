@@ -1,0 +1,293 @@
+"""Adjoint-state FWI objective and gradient on the GPU (the PDEfunc OBJ / FORW_MODEL path).
+
+Mirrors ``[f,g] = PDEfunc(PDEopts.OBJ, v, Q, [], Dobs, model, params)`` and
+``D = PDEfunc(PDEopts.FORW_MODEL, ...)`` for 3D grids
+(tools/algorithms/CommonFreqModeling/PDEfunc.m:254-394):
+
+  per frequency k:  wn, dwn = param2wavenum(Pext v, f_k, unit)          (discrete_helmholtz.m:240-257)
+  per source s:     q   = Ps (w(f_k) Q_s) prod(d)/prod(dt)               (PDEfunc.m:330-339)
+                    U   = H \\ q                                          (PDEfunc.m:347)
+                    phi, dphi = LS_misfit(Pr U, D_obs)                    (PDEfunc.m:389, LS_misfit.m:23-25)
+                    V   = H' \\ (-Pr' dphi)                               (PDEfunc.m:393)
+                    g  += crop( Re(conj(U) .* (dH' V)) )                  (PDEfunc.m:394, discrete_helmholtz.m:288)
+
+The sources of one frequency are solved together as one batch of right-hand sides; the
+gradient accumulation over the batch is one fused kernel (h3d_grad_accum).  Forward
+wavefields are kept for the gradient while they fit an HBM budget and recomputed
+otherwise.  Everything runs through libh3d.so's C ABI.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import solver as S
+
+
+def param2wavenum(v: torch.Tensor, freq: float, unit: str):
+    """(wn, dwn) = ((2 pi f)^2 * m, derivative) as in param2wavenum.m:20-49."""
+    c = (2.0 * np.pi * freq) ** 2
+    if unit == "m/s":
+        return c * v.pow(-2), -2.0 * c * v.pow(-3)
+    if unit == "s2/m2":
+        return c * v, torch.full_like(v, c)
+    if unit == "s2/km2":
+        return 1e-6 * c * v, torch.full_like(v, 1e-6 * c)
+    raise ValueError(f"Unknown unit - {unit}")
+
+
+def extend_edges(v: torch.Tensor, npml6) -> torch.Tensor:
+    """opExtension mode 1 in 3D (edge replication), v indexed (x, y, z)."""
+    lx, hx, ly, hy, lz, hz = (int(p) for p in npml6)
+    t = v.permute(2, 1, 0)[None, None]                         # (1,1,z,y,x)
+    t = torch.nn.functional.pad(t, (lx, hx, ly, hy, lz, hz), mode="replicate")
+    return t[0, 0].permute(2, 1, 0).contiguous()
+
+
+def fwi_wavelet(freqs, t0: float, f0: float):
+    f = np.asarray(freqs, dtype=np.float64)
+    w = np.exp(-1j * 2 * np.pi * f * t0)
+    if f0:
+        w = f ** 2 * np.exp(-(f / f0) ** 2) * w
+    return w
+
+
+def _flat(v3: torch.Tensor) -> torch.Tensor:
+    """(x,y,z) array -> x-fastest flat vector (column-major, the reference layout)."""
+    return v3.permute(2, 1, 0).contiguous().reshape(-1)
+
+
+def _unflat(v: torch.Tensor, n) -> torch.Tensor:
+    return v.reshape(n[2], n[1], n[0]).permute(2, 1, 0)
+
+
+@dataclass
+class Geometry:
+    """Physical grid and acquisition: origin o, spacing d (m), interior size n, PML widths."""
+    o: tuple
+    d: tuple
+    n: tuple
+    npml6: tuple
+    src_xyz: np.ndarray             # (nsrc, 3) physical coordinates (m)
+    rec_xyz: np.ndarray             # (nrec, 3)
+    freqs: np.ndarray
+    f0: float = 8.0
+    t0: float = 0.0
+    unit: str = "m/s"
+    src_amp: np.ndarray | None = None   # per-source complex amplitude (Q); ones by default
+
+    @property
+    def n_total(self):
+        p = self.npml6
+        return (self.n[0] + p[0] + p[1], self.n[1] + p[2] + p[3], self.n[2] + p[4] + p[5])
+
+    def grid(self) -> L.Grid:
+        return L.make_grid(self.n_total, self.d, self.npml6)
+
+    def to_index(self, xyz: np.ndarray) -> np.ndarray:
+        """Physical coordinates -> computational-grid index units (ot = o - npml_lo d)."""
+        xyz = np.asarray(xyz, dtype=np.float64).reshape(-1, 3)
+        ot = np.array([self.o[a] - self.npml6[2 * a] * self.d[a] for a in range(3)])
+        return (xyz - ot) / np.asarray(self.d, dtype=np.float64)
+
+
+class _Interp:
+    """Device-resident separable sinc-Kaiser weights of a point set (h3d_sinc_weights)."""
+
+    def __init__(self, g: L.Grid, pts_idx: np.ndarray, dev):
+        n = pts_idx.shape[0]
+        base = np.zeros((n, 3), np.int32)
+        w = np.zeros((n, 3, 9))
+        pts = np.ascontiguousarray(pts_idx, dtype=np.float64)
+        rc = L.load().h3d_sinc_weights(C.byref(g), pts.ctypes.data_as(C.POINTER(C.c_double)), n,
+                                       base.ctypes.data_as(C.POINTER(C.c_int32)),
+                                       w.ctypes.data_as(C.POINTER(C.c_double)))
+        L.check(rc, "h3d_sinc_weights")
+        self.n = n
+        self.base = torch.as_tensor(base, device=dev)
+        self.w = torch.as_tensor(w, device=dev)
+
+
+def _stream():
+    return C.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+@dataclass
+class FWIConfig:
+    tol: float = 1e-6
+    maxit: int = 10000
+    precision: str = "mixed"
+    order: str = "colour27"
+    hbm_budget_bytes: float = 40e9        # keep forward wavefields up to this size
+    src_batch: int = 0                    # 0 = all sources of a frequency in one batch
+    extra: dict = field(default_factory=dict)
+
+
+class FWIProblem:
+    """PDEfunc-style forward modelling, objective and gradient on one GPU."""
+
+    def __init__(self, geom: Geometry, cfg: FWIConfig | None = None, device="cuda:0"):
+        self.geom = geom
+        self.cfg = cfg or FWIConfig()
+        self.dev = torch.device(device)
+        self.g = geom.grid()
+        self.N = int(np.prod(geom.n_total))
+        self.src = _Interp(self.g, geom.to_index(geom.src_xyz), self.dev)
+        self.rec = _Interp(self.g, geom.to_index(geom.rec_xyz), self.dev)
+        self.nsrc, self.nrec = self.src.n, self.rec.n
+        amp = geom.src_amp if geom.src_amp is not None else np.ones(self.nsrc)
+        self.src_amp = np.asarray(amp, dtype=np.complex128)
+        self.wavelet = fwi_wavelet(geom.freqs, geom.t0, geom.f0)
+        self.last_infos: list = []
+
+    # -- pieces -------------------------------------------------------------------------------
+    def _opts(self):
+        c = self.cfg
+        return S.make_opts(tol=c.tol, maxit=c.maxit, precision=c.precision, order=c.order, **c.extra)
+
+    def _wavenumbers(self, v_phys: torch.Tensor, freq: float):
+        v = extend_edges(v_phys.to(self.dev, torch.float64), self.geom.npml6)
+        wn, dwn = param2wavenum(v, freq, self.geom.unit)
+        return _flat(wn), _flat(dwn)
+
+    def _sources(self, k: int, srcs) -> torch.Tensor:
+        """Q_k for the listed sources: (len(srcs), N) complex128."""
+        ns = len(srcs)
+        b = torch.zeros(ns, self.N, dtype=torch.complex128, device=self.dev)
+        scale = self.wavelet[k] * self.src_amp[srcs] * (np.prod(self.geom.d) / np.prod(self.geom.d))
+        sc = torch.as_tensor(np.stack([scale.real, scale.imag], 1), device=self.dev).contiguous()
+        base = self.src.base[srcs].contiguous()
+        w = self.src.w[srcs].contiguous()
+        rc = L.load().h3d_src_inject(C.byref(self.g), C.c_void_p(base.data_ptr()),
+                                     C.c_void_p(w.data_ptr()), C.c_void_p(sc.data_ptr()),
+                                     C.c_void_p(b.data_ptr()), ns, _stream())
+        L.check(rc, "h3d_src_inject")
+        return b
+
+    def _sample(self, U: torch.Tensor) -> torch.Tensor:
+        P = U.shape[0]
+        d = torch.empty(P, self.nrec, dtype=torch.complex128, device=self.dev)
+        rc = L.load().h3d_rec_sample(C.byref(self.g), C.c_void_p(self.rec.base.data_ptr()),
+                                     C.c_void_p(self.rec.w.data_ptr()), self.nrec,
+                                     C.c_void_p(U.data_ptr()), P, C.c_void_p(d.data_ptr()), _stream())
+        L.check(rc, "h3d_rec_sample")
+        return d
+
+    def _spread(self, D: torch.Tensor, scale: float) -> torch.Tensor:
+        P = D.shape[0]
+        D = D.contiguous()
+        b = torch.empty(P, self.N, dtype=torch.complex128, device=self.dev)
+        rc = L.load().h3d_rec_spread(C.byref(self.g), C.c_void_p(self.rec.base.data_ptr()),
+                                     C.c_void_p(self.rec.w.data_ptr()), self.nrec,
+                                     C.c_void_p(D.data_ptr()), P, float(scale),
+                                     C.c_void_p(b.data_ptr()), _stream())
+        L.check(rc, "h3d_rec_spread")
+        return b
+
+    def _grad_accum(self, dwn, U, V, gphys: torch.Tensor, scale=1.0):
+        rc = L.load().h3d_grad_accum(C.byref(self.g), C.c_void_p(dwn.data_ptr()),
+                                     C.c_void_p(U.data_ptr()), C.c_void_p(V.data_ptr()), U.shape[0],
+                                     float(scale), C.c_void_p(gphys.data_ptr()), _stream())
+        L.check(rc, "h3d_grad_accum")
+
+    def _batches(self):
+        bs = self.cfg.src_batch or self.nsrc
+        return [list(range(s, min(s + bs, self.nsrc))) for s in range(0, self.nsrc, bs)]
+
+    def _solve(self, wn, b, mode):
+        u, info = S.solve(self.g, wn, b, mode=mode, opts=self._opts())
+        self.last_infos.append(info)
+        return u
+
+    # -- PDEfunc FORW_MODEL ----------------------------------------------------------------------
+    def forward_model(self, v_phys: torch.Tensor, return_fields: bool = False):
+        """D (nrec x nsrc*nfreq), column = src + nsrc*freq (PDEfunc.m:341,423)."""
+        cols, fields = [], []
+        for k, fr in enumerate(self.geom.freqs):
+            wn, _ = self._wavenumbers(v_phys, float(fr))
+            for srcs in self._batches():
+                U = self._solve(wn, self._sources(k, srcs), 1)
+                cols.append(self._sample(U))
+                if return_fields:
+                    fields.append(U)
+        D = torch.cat(cols, 0).T.contiguous()
+        return (D, fields) if return_fields else D
+
+    # -- PDEfunc OBJ -----------------------------------------------------------------------------
+    def wavefield_bytes(self) -> float:
+        return 16.0 * self.N * self.nsrc * len(self.geom.freqs)
+
+    def misfit_forward(self, v_phys: torch.Tensor, Dobs: torch.Tensor, keep: bool):
+        """f and the data residuals; keeps the forward wavefields when ``keep``."""
+        f = 0.0
+        resid, fields = [], []
+        col = 0
+        for k, fr in enumerate(self.geom.freqs):
+            wn, _ = self._wavenumbers(v_phys, float(fr))
+            for srcs in self._batches():
+                U = self._solve(wn, self._sources(k, srcs), 1)
+                dpred = self._sample(U)
+                dobs = Dobs[:, col:col + len(srcs)].T.to(torch.complex128)
+                r = dpred - dobs                                     # LS_misfit.m:23
+                f += 0.5 * float(torch.sum(r.real ** 2 + r.imag ** 2))   # LS_misfit.m:24
+                resid.append(r)
+                fields.append(U if keep else None)
+                col += len(srcs)
+        return f, resid, fields
+
+    def gradient(self, v_phys: torch.Tensor, resid, fields):
+        """g (physical grid, x-fastest flat) from the residuals; recomputes U where not kept."""
+        n = self.geom.n
+        g = torch.zeros(int(np.prod(n)), dtype=torch.float64, device=self.dev)
+        q = 0
+        for k, fr in enumerate(self.geom.freqs):
+            wn, dwn = self._wavenumbers(v_phys, float(fr))
+            for srcs in self._batches():
+                U = fields[q]
+                if U is None:
+                    U = self._solve(wn, self._sources(k, srcs), 1)   # recompute above the budget
+                V = self._solve(wn, self._spread(resid[q], -1.0), 2)   # H' \ (-Pr' dphi)
+                self._grad_accum(dwn, U, V, g)
+                q += 1
+        return g
+
+    def objective(self, v_phys: torch.Tensor, Dobs: torch.Tensor):
+        """(f, g) as PDEfunc OBJ (no 1/#pairs scaling; misfit_setup applies that)."""
+        keep = self.wavefield_bytes() <= self.cfg.hbm_budget_bytes
+        f, resid, fields = self.misfit_forward(v_phys, Dobs, keep)
+        g = self.gradient(v_phys, resid, fields)
+        return f, _unflat(g, self.geom.n)
+
+
+class FWIObjective(torch.autograd.Function):
+    """f(m) with the adjoint-state gradient as its backward.
+
+    forward: forward solves + misfit (wavefields kept within the HBM budget);
+    backward: adjoint solves and the fused gradient accumulation, recomputing the
+    forward wavefields when they were not kept.
+    """
+
+    @staticmethod
+    def forward(ctx, m: torch.Tensor, problem: FWIProblem, Dobs: torch.Tensor):
+        keep = problem.wavefield_bytes() <= problem.cfg.hbm_budget_bytes
+        f, resid, fields = problem.misfit_forward(m.detach(), Dobs, keep)
+        ctx.problem = problem
+        ctx.resid = resid
+        ctx.fields = fields
+        ctx.save_for_backward(m)
+        return torch.tensor(f, dtype=torch.float64, device=m.device)
+
+    @staticmethod
+    def backward(ctx, gf):
+        (m,) = ctx.saved_tensors
+        g = ctx.problem.gradient(m.detach(), ctx.resid, ctx.fields)
+        ctx.resid = ctx.fields = None
+        return gf * _unflat(g, ctx.problem.geom.n).to(m.dtype), None, None
+
+
+def fwi_objective(m: torch.Tensor, problem: FWIProblem, Dobs: torch.Tensor) -> torch.Tensor:
+    return FWIObjective.apply(m, problem, Dobs)
