@@ -114,7 +114,10 @@ typedef struct h3d_solve_info {
     double rel_res_true;    /* max over RHS of ||b - H u|| / ||b|| (FP64), or -1 if not computed */
     double rel_res_prec;    /* max over RHS of the last preconditioned residual ratio */
     double seconds;         /* wall time of the call (host clock, after stream sync) */
-    double sweep_seconds;   /* device time in sweep kernels, if measured (else 0) */
+    double sweep_seconds;   /* sum of the sampled double-sweep device times (CUDA events) */
+    int32_t sweep_samples;  /* number of double sweeps timed (one per replayed iteration block) */
+    int32_t pad_;
+    int64_t kernel_launches;/* device kernels this call executed (graph replays included) */
 } h3d_solve_info;
 
 /* One problem of a batched solve: its own grid, wavenumber and right-hand sides. */

@@ -121,10 +121,34 @@ struct CgRun {
     DevBuf vecs, scal, ints, parts;
     cudaGraphExec_t exec = nullptr;
     int graph_iters = 0;
+    // Timing of the last double sweep of every replayed block: two timing events recorded
+    // as event nodes of the graph, read after the block completes.
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    bool timed_pending = false;
+    double sweep_seconds = 0.0;
+    int sweep_samples = 0;
+    long long launches = 0;        // kernels executed by this instance
+    long long block_launches = 0;  // kernels in one replayed block
 
     ~CgRun()
     {
         if (exec) cudaGraphExecDestroy(exec);
+        if (ev0) cudaEventDestroy(ev0);
+        if (ev1) cudaEventDestroy(ev1);
+    }
+
+    int iteration_launches() const { return sweep_launches() + 5; }
+
+    // Fold the last timed sweep into the totals (the stream has been synchronised).
+    void harvest_timing()
+    {
+        if (!timed_pending) return;
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) {
+            sweep_seconds += 1e-3 * ms;
+            ++sweep_samples;
+        }
+        timed_pending = false;
     }
 
     int alloc(cudaStream_t st)
@@ -158,13 +182,19 @@ struct CgRun {
 
     int sweep_launches() const
     {
-        if (order == H3D_ORDER_LEX) return 2 * (op.nx + 3 * op.ny + 9 * op.nz);
+        if (order == H3D_ORDER_LEX) return 2 * ((op.nx - 1) + 3 * (op.ny - 1) + 9 * (op.nz - 1) + 1);
         if (order == H3D_ORDER_BLOCK) {
             const int bx = block[0] > 0 ? block[0] : 8, by = block[1] > 0 ? block[1] : 8,
                       bz = block[2] > 0 ? block[2] : 8;
-            return 2 * ((op.nx + bx - 1) / bx + 2 * ((op.ny + by - 1) / by) + 4 * ((op.nz + bz - 1) / bz));
+            return 2 * (((op.nx + bx - 1) / bx - 1) + 2 * ((op.ny + by - 1) / by - 1) +
+                        4 * ((op.nz + bz - 1) / bz - 1) + 1);
         }
-        return 54;
+        int n = 0;
+        for (int q = 0; q < 27; ++q) {
+            const int a = q % 3, bq = (q / 3) % 3, cq = q / 9;
+            n += (op.nx > a && op.ny > bq && op.nz > cq) ? 1 : 0;
+        }
+        return 2 * n;
     }
 
     // b~ = DSWP(0, b) into y, then x = 0, r = p = y.
@@ -173,13 +203,16 @@ struct CgRun {
         int rc;
         if ((rc = zero_vec<T>(y, N, nrhs, st))) return rc;
         if ((rc = launch_sweep<T>(op, y, b, nrhs, w, adj, order, block, nullptr, st))) return rc;
+        launches += sweep_launches() + 2;
         return cg_init<T>(y, x, r, p, N, nrhs, s, bnorm2_orig, zero_tol2, maxit, st);
     }
 
-    int enqueue_iteration(cudaStream_t st)
+    int enqueue_iteration(cudaStream_t st, bool timed)
     {
         int rc;
+        if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev0, st, cudaEventRecordExternal));
         if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st))) return rc;
+        if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev1, st, cudaEventRecordExternal));
         if ((rc = cg_ap_dot<T>(p, y, N, nrhs, s, st))) return rc;
         if ((rc = cg_update_xr<T>(x, r, p, y, N, nrhs, s, maxit, st))) return rc;
         return cg_update_p<T>(p, r, y, N, nrhs, s, st);
@@ -187,11 +220,18 @@ struct CgRun {
 
     int run_block(int iters, bool use_graph, cudaStream_t st)
     {
+        if (!ev0) {
+            H3D_CUDA_TRY(cudaEventCreate(&ev0));
+            H3D_CUDA_TRY(cudaEventCreate(&ev1));
+        }
+        block_launches = (long long)iters * iteration_launches();
         if (!use_graph) {
             for (int q = 0; q < iters; ++q) {
-                int rc = enqueue_iteration(st);
+                int rc = enqueue_iteration(st, q == iters - 1);
                 if (rc) return rc;
             }
+            launches += block_launches;
+            timed_pending = true;
             return H3D_OK;
         }
         if (!exec || graph_iters != iters) {
@@ -200,7 +240,7 @@ struct CgRun {
             cudaGraph_t g = nullptr;
             H3D_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
             int rc = H3D_OK;
-            for (int q = 0; q < iters && !rc; ++q) rc = enqueue_iteration(st);
+            for (int q = 0; q < iters && !rc; ++q) rc = enqueue_iteration(st, q == iters - 1);
             cudaError_t e = cudaStreamEndCapture(st, &g);
             if (rc) {
                 if (g) cudaGraphDestroy(g);
@@ -213,6 +253,8 @@ struct CgRun {
             graph_iters = iters;
         }
         H3D_CUDA_TRY(cudaGraphLaunch(exec, st));
+        launches += block_launches;
+        timed_pending = true;
         return H3D_OK;
     }
 };
@@ -268,6 +310,7 @@ static int cg_drive(CgRun<T> &cg, HostState &hs, const h3d_solve_opts &o, double
     for (;;) {
         int rc = hs.fetch(cg, st);
         if (rc) return rc;
+        cg.harvest_timing();
         bool any = false;
         double mx = 0.0;
         for (int q = 0; q < hs.n; ++q) {
@@ -318,6 +361,10 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
     double *rr2 = normb.as<double>(), *bb2 = rr2 + nrhs;
     H3D_CUDA_TRY(cudaMemsetAsync(u, 0, sizeof(cplx<double>) * (size_t)N * nrhs, st));
     if ((rc = residual_f64(op64, b, u, r64, rr2, bb2, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
+    long long extra_launches = 2;
+    double sw_sec = 0.0;
+    int sw_n = 0;
+    long long cg_launches = 0;
 
     std::vector<double> h_rr(nrhs), h_bb(nrhs);
     auto fetch_norms = [&]() -> int {
@@ -359,6 +406,7 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
             if ((rc = cg_drive(cg, hs, o, res_hist, res_hist_len, &hist_pos, st))) return rc;
             ++outer;
             if ((rc = residual_f64(op64, b, cg.x, r64, rr2, nullptr, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
+            extra_launches += 2;
             if ((rc = fetch_norms())) return rc;
             if (o.stop_rule != H3D_STOP_TRUE_RESIDUAL) break;
             bool again = false;
@@ -386,6 +434,9 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
             last_prec = std::max(last_prec, hs.ratio[q]);
             nonfinite |= hs.status[q] != 0;
         }
+        sw_sec = cg.sweep_seconds;
+        sw_n = cg.sweep_samples;
+        cg_launches = cg.launches;
     } else {
         // Mixed precision: complex64 CGMN on the scaled FP64 residual, FP64 update and residual.
         DevBuf wn32b, rhs32b;
@@ -393,6 +444,7 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         float *wn32 = wn32b.as<float>();
         if ((rc = cast<double, float>(wn_re, wn32, N, st))) return rc;
         if (wn_im && (rc = cast<double, float>(wn_im, wn32 + N, N, st))) return rc;
+        extra_launches += wn_im ? 2 : 1;
         Op<float> op32;
         if ((rc = make_op_f32(g, wn32, wn_im ? wn32 + N : nullptr, &op32))) return rc;
         if ((rc = rhs32b.alloc(sizeof(cplx<float>) * (size_t)N * nrhs, st))) return rc;
@@ -434,9 +486,13 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
                 nonfinite |= hs.status[q] != 0;
             }
             if ((rc = residual_f64(op64, b, u, r64, rr2, nullptr, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
+            extra_launches += 4;  // scale, add, residual (2)
             if ((rc = fetch_norms())) return rc;
             if (nonfinite) break;
         }
+        sw_sec = cg.sweep_seconds;
+        sw_n = cg.sweep_samples;
+        cg_launches = cg.launches;
     }
     bool all_ok = !nonfinite;
     double worst = 0.0;
@@ -459,7 +515,10 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         info->rel_res_true = worst;
         info->rel_res_prec = last_prec;
         info->seconds = timer.seconds();
-        info->sweep_seconds = 0.0;
+        info->sweep_seconds = sw_sec;
+        info->sweep_samples = sw_n;
+        info->pad_ = 0;
+        info->kernel_launches = extra_launches + cg_launches;
     }
     if (nonfinite) {
         set_error("non-finite value in the CGMN iteration");

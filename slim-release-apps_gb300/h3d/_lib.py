@@ -41,11 +41,12 @@ class SolveInfo(C.Structure):
     _fields_ = [
         ("iters", C.c_int32), ("outer", C.c_int32), ("converged", C.c_int32), ("nrhs", C.c_int32),
         ("rel_res_true", C.c_double), ("rel_res_prec", C.c_double), ("seconds", C.c_double),
-        ("sweep_seconds", C.c_double),
+        ("sweep_seconds", C.c_double), ("sweep_samples", C.c_int32), ("pad_", C.c_int32),
+        ("kernel_launches", C.c_int64),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_}
+        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
 
 
 class Problem(C.Structure):
