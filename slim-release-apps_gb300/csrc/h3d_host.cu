@@ -192,6 +192,49 @@ static int make_op(const h3d_grid *g, const T *wn, const T *wni, Op<T> *op)
     o.xz = (T)(kW2 / (2 * hxz));
     o.xy = (T)(kW2 / (2 * hxy));
     o.yz = (T)(kW2 / (2 * hyz));
+    // Interior class constants: the PML terms with every xi_lo = xi_hi = 1 (so each
+    // per-axis sum is 2), in the offset classes [centre, face x/y/z, edge xy/xz/yz, corner].
+    o.kint[0] = (T)(2 * ((double)o.wn_x + (double)o.wn_y + (double)o.wn_z));
+    o.kint[1] = (T)((double)o.pml_x + 2 * (double)o.xz + 2 * (double)o.xy);
+    o.kint[2] = (T)((double)o.pml_y + 2 * (double)o.yz + 2 * (double)o.xy);
+    o.kint[3] = (T)((double)o.pml_z + 2 * (double)o.yz + 2 * (double)o.xz);
+    o.kint[4] = (T)(-2 * (double)o.xy + 2 * (double)o.w3a2);
+    o.kint[5] = (T)(-2 * (double)o.xz + 2 * (double)o.w3a2);
+    o.kint[6] = (T)(-2 * (double)o.yz + 2 * (double)o.w3a2);
+    o.kint[7] = (T)(-3 * (double)o.w3a2);
+    // Row ranges whose PML values are exactly 1 (and whose neighbours are all inside the
+    // grid), from the same FP64 tables the kernels use.
+    {
+        std::vector<std::complex<double>> tab;
+        int lo[3], hi[3], sum[3];
+        fill_tables(g, tab, lo, hi, sum);
+        const std::complex<double> one(1.0, 0.0), two(2.0, 0.0);
+        for (int a = 0; a < 3; ++a) {
+            const int n = g->n[a];
+            auto fwd = [&](int i) { return tab[lo[a] + i + 1] == one && tab[hi[a] + i + 1] == one; };
+            auto adj = [&](int i) {
+                return tab[hi[a] + i] == one && tab[lo[a] + i + 2] == one && tab[sum[a] + i + 1] == two;
+            };
+            for (int pass = 0; pass < 2; ++pass) {
+                int first = -1, last = -2;
+                for (int i = 1; i < n - 1; ++i)
+                    if (pass == 0 ? fwd(i) : adj(i)) {
+                        if (first < 0) first = i;
+                        last = i;
+                    }
+                bool contiguous = first >= 0;
+                for (int i = first; contiguous && i <= last; ++i) contiguous = pass == 0 ? fwd(i) : adj(i);
+                const int l = contiguous ? first : 0, h = contiguous ? last + 1 : 0;
+                if (pass == 0) {
+                    o.int_lo_f[a] = l;
+                    o.int_hi_f[a] = h;
+                } else {
+                    o.int_lo_a[a] = l;
+                    o.int_hi_a[a] = h;
+                }
+            }
+        }
+    }
     *op = o;
     return H3D_OK;
 }

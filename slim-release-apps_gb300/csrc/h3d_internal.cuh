@@ -69,6 +69,13 @@ struct Op {
     T pml_x, pml_y, pml_z;       // face coefficients
     T xz, xy, yz;                // cross coefficients
     T w3a2;                      // corner coefficient
+    // Interior (all xi = 1): PML part of the coefficient per offset class
+    // [centre, face x, face y, face z, edge xy, edge xz, edge yz, corner].
+    T kint[8];
+    // Row index ranges [lo, hi) per axis whose PML values are all 1, for the forward
+    // rows (xi_lo(i) = xi_hi(i) = 1) and the adjoint rows (xi_hi(i-1) = xi_lo(i+1) = 1
+    // and xi_lo(i) + xi_hi(i) = 2).
+    int int_lo_f[3], int_hi_f[3], int_lo_a[3], int_hi_a[3];
 };
 
 // Enumerate the 27 stencil offsets: t = (dx+1) + 3(dy+1) + 9(dz+1) (Helm3d_27pt.h:163-189).
@@ -138,50 +145,111 @@ __device__ __forceinline__ uint32_t inside_mask(int i, int j, int k, int nx, int
 //  adjoint (Helm3d_27pt.h:716-822): c_t = conj(-WM_t wn[row] + pml_term(t) evaluated at the
 //    neighbour row), not masked;
 //  DERIV (Helm3d_27pt.h:202-206, 754): the PML part is dropped.
+// PML values one row needs: the per-axis sums S and the directional values A for the
+// -1 and +1 offsets (forward: xi_lo(c), xi_hi(c); adjoint: xi_hi(c-1), xi_lo(c+1), the
+// windows of pml_adj_info, Helm3d_27pt.h:252-260, 394-465).
+template <typename T>
+struct RowPml {
+    cplx<T> Sx, Sy, Sz, Axm, Axp, Aym, Ayp, Azm, Azp;
+};
+
+template <typename T, bool ADJ>
+__device__ __forceinline__ RowPml<T> load_row_pml(const Op<T> &op, int i, int j, int k)
+{
+    const cplx<T> *t = op.tab;
+    RowPml<T> p;
+    p.Sx = t[op.sum[0] + i + 1];
+    p.Sy = t[op.sum[1] + j + 1];
+    p.Sz = t[op.sum[2] + k + 1];
+    if constexpr (!ADJ) {
+        p.Axm = t[op.lo[0] + i + 1]; p.Axp = t[op.hi[0] + i + 1];
+        p.Aym = t[op.lo[1] + j + 1]; p.Ayp = t[op.hi[1] + j + 1];
+        p.Azm = t[op.lo[2] + k + 1]; p.Azp = t[op.hi[2] + k + 1];
+    } else {
+        p.Axm = t[op.hi[0] + i]; p.Axp = t[op.lo[0] + i + 2];
+        p.Aym = t[op.hi[1] + j]; p.Ayp = t[op.lo[1] + j + 2];
+        p.Azm = t[op.hi[2] + k]; p.Azp = t[op.lo[2] + k + 2];
+    }
+    return p;
+}
+
+// Coefficient of one offset (T = 0..26 fixed at compile time).
+template <int TT, int DX, int DY, int DZ, typename T, bool ADJ, bool DERIV, bool WNC, typename WnF>
+__device__ __forceinline__ cplx<T> coef_at(const Op<T> &op, const RowPml<T> &p, uint32_t inmask,
+                                           WnF wnf)
+{
+    const cplx<T> Ax = DX < 0 ? p.Axm : p.Axp, Ay = DY < 0 ? p.Aym : p.Ayp, Az = DZ < 0 ? p.Azm : p.Azp;
+    cplx<T> v;
+    if constexpr (!ADJ) {
+        if (inmask & (1u << TT)) {
+            const cplx<T> wv = wnf(DX, DY, DZ);
+            v = (TT == 13) ? op.wn_c * wv : T(-WM<DX, DY, DZ>::value) * wv;
+            if constexpr (!DERIV) v = v + pml_term<DX, DY, DZ, T>(op, Ax, Ay, Az, p.Sx, p.Sy, p.Sz);
+        } else {
+            v = mk<T>(T(0), T(0));
+        }
+    } else {
+        const cplx<T> wc = wnf(0, 0, 0);
+        v = (TT == 13) ? op.wn_c * wc : T(-WM<DX, DY, DZ>::value) * wc;
+        if constexpr (!DERIV) v = v + pml_term<DX, DY, DZ, T>(op, Ax, Ay, Az, p.Sx, p.Sy, p.Sz);
+        v = cconj(v);
+    }
+    return v;
+}
+
+// The wavenumber of neighbour (dx,dy,dz) comes from a caller-supplied accessor
+// wnf(dx, dy, dz) -> cplx<T> (global memory or a shared-memory tile).
+template <typename T, bool ADJ, bool DERIV, bool WNC, typename WnF>
+__device__ __forceinline__ void row_coefs_with(const Op<T> &op, int i, int j, int k,
+                                               uint32_t inmask, WnF wnf, cplx<T> c[27])
+{
+    RowPml<T> p{};
+    if constexpr (!DERIV) p = load_row_pml<T, ADJ>(op, i, j, k);
+#define H3D_COEF2(t, dx, dy, dz) c[t] = coef_at<t, dx, dy, dz, T, ADJ, DERIV, WNC>(op, p, inmask, wnf);
+    H3D_FOR_27(H3D_COEF2)
+#undef H3D_COEF2
+}
+
+// Real coefficients of a row whose PML values are all xi_lo = xi_hi = 1 (the interior):
+// c_t = K_t - WM_t * wn_t with the class constants K_t of Op::kint (forward: wn of the
+// neighbour; adjoint: wn of the centre, and conj is the identity for real values).
+template <typename T, bool ADJ, typename WnR>
+__device__ __forceinline__ void row_coefs_interior(const Op<T> &op, WnR wnr, T c[27])
+{
+    const T wc = wnr(0, 0, 0);
+#define H3D_COEF_INT(t, dx, dy, dz)                                                            \
+    {                                                                                          \
+        constexpr int nzc = (dx != 0) + (dy != 0) + (dz != 0);                                 \
+        constexpr int cls = nzc == 0 ? 0 : nzc == 3 ? 7                                        \
+                          : nzc == 1 ? (dx ? 1 : dy ? 2 : 3) : (!dz ? 4 : !dy ? 5 : 6);        \
+        const T wv = ADJ ? wc : ((t == 13) ? wc : wnr(dx, dy, dz));                            \
+        c[t] = (t == 13) ? (op.wn_c * wv + op.kint[0]) : (op.kint[cls] - T(WM<dx, dy, dz>::value) * wv); \
+    }
+    H3D_FOR_27(H3D_COEF_INT)
+#undef H3D_COEF_INT
+}
+
+// One interior coefficient (see row_coefs_interior).
+template <int TT, int DX, int DY, int DZ, typename T, bool ADJ, typename WnR>
+__device__ __forceinline__ T coef_int(const Op<T> &op, WnR wnr)
+{
+    constexpr int nzc = (DX != 0) + (DY != 0) + (DZ != 0);
+    constexpr int cls = nzc == 0 ? 0 : nzc == 3 ? 7 : nzc == 1 ? (DX ? 1 : DY ? 2 : 3) : (!DZ ? 4 : !DY ? 5 : 6);
+    const T wv = ADJ ? wnr(0, 0, 0) : wnr(DX, DY, DZ);
+    if constexpr (TT == 13) return op.wn_c * wv + op.kint[0];
+    else return op.kint[cls] - T(WM<DX, DY, DZ>::value) * wv;
+}
+
 template <typename T, bool ADJ, bool DERIV, bool WNC>
 __device__ __forceinline__ void row_coefs(const Op<T> &op, int i, int j, int k, uint32_t inmask,
                                           cplx<T> c[27])
 {
     const long long ctr = i + op.sy * j + op.sz * k;
-    cplx<T> Sx{}, Sy{}, Sz{}, Axm{}, Axp{}, Aym{}, Ayp{}, Azm{}, Azp{};
-    if constexpr (!DERIV) {
-        const cplx<T> *t = op.tab;
-        Sx = t[op.sum[0] + i + 1];
-        Sy = t[op.sum[1] + j + 1];
-        Sz = t[op.sum[2] + k + 1];
-        if constexpr (!ADJ) {
-            Axm = t[op.lo[0] + i + 1]; Axp = t[op.hi[0] + i + 1];
-            Aym = t[op.lo[1] + j + 1]; Ayp = t[op.hi[1] + j + 1];
-            Azm = t[op.lo[2] + k + 1]; Azp = t[op.hi[2] + k + 1];
-        } else {
-            // xi_hi of the left neighbour, xi_lo of the right neighbour (pml_adj_info windows)
-            Axm = t[op.hi[0] + i]; Axp = t[op.lo[0] + i + 2];
-            Aym = t[op.hi[1] + j]; Ayp = t[op.lo[1] + j + 2];
-            Azm = t[op.hi[2] + k]; Azp = t[op.lo[2] + k + 2];
-        }
-    }
-    const cplx<T> wc = load_wn<T, WNC>(op, ctr);
-#define H3D_COEF(t, dx, dy, dz)                                                                \
-    {                                                                                          \
-        const cplx<T> Ax = dx < 0 ? Axm : Axp, Ay = dy < 0 ? Aym : Ayp, Az = dz < 0 ? Azm : Azp; \
-        cplx<T> v;                                                                             \
-        if constexpr (!ADJ) {                                                                  \
-            if (inmask & (1u << t)) {                                                          \
-                const cplx<T> wv = (t == 13) ? wc : load_wn<T, WNC>(op, ctr + dx + op.sy * dy + op.sz * dz); \
-                v = (t == 13) ? op.wn_c * wv : T(-WM<dx, dy, dz>::value) * wv;                 \
-                if constexpr (!DERIV) v = v + pml_term<dx, dy, dz, T>(op, Ax, Ay, Az, Sx, Sy, Sz); \
-            } else {                                                                           \
-                v = mk<T>(T(0), T(0));                                                         \
-            }                                                                                  \
-        } else {                                                                               \
-            v = (t == 13) ? op.wn_c * wc : T(-WM<dx, dy, dz>::value) * wc;                     \
-            if constexpr (!DERIV) v = v + pml_term<dx, dy, dz, T>(op, Ax, Ay, Az, Sx, Sy, Sz);  \
-            v = cconj(v);                                                                      \
-        }                                                                                      \
-        c[t] = v;                                                                              \
-    }
-    H3D_FOR_27(H3D_COEF)
-#undef H3D_COEF
+    row_coefs_with<T, ADJ, DERIV, WNC>(op, i, j, k, inmask,
+                                       [&](int dx, int dy, int dz) {
+                                           return load_wn<T, WNC>(op, ctr + dx + op.sy * dy + op.sz * dz);
+                                       },
+                                       c);
 }
 
 // ---------------------------------------------------------------------------------------

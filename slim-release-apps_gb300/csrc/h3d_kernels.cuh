@@ -21,13 +21,31 @@ __device__ __forceinline__ cplx<float> load_cg(const cplx<float> *p)
     return {v.x, v.y};
 }
 
-// h3d_stencil.cu
+// h3d_mvp.cu: z-marching matvec, and the FP64 residual b - A x with per-block norms.
+int mvp_residual_parts(const Op<double> &op, int nrhs);
+int launch_residual(const Op<double> &op, const cplx<double> *b, const cplx<double> *x, cplx<double> *r,
+                    int nrhs, bool adj, double *part, cudaStream_t st);
+
+// h3d_mvp.cu / h3d_stencil.cu
 template <typename T>
 int launch_mvp(const Op<T> &op, const cplx<T> *x, cplx<T> *y, int nrhs, bool adj, bool deriv,
                cudaStream_t st);
+// rinv: optional 1/||a_i||^2 per row (COLOUR27 only; NULL = computed in the kernel);
+// shape: COLOUR27 tile shape index (-1 = chosen from the grid).
 template <typename T>
 int launch_sweep(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, bool adj,
-                 int order, const int32_t *block, const int *active, cudaStream_t st);
+                 int order, const int32_t *block, const int *active, cudaStream_t st,
+                 const T *rinv = nullptr, int shape = -1);
+
+// h3d_sweep_tile.cu: one COLOUR27 pass (27 colour launches) with shared-memory boxes.
+template <typename T>
+int sweep_colour_tiled(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w,
+                       const int *active, const T *rinv, int shape, bool adj, bool backward,
+                       cudaStream_t st);
+template <typename T>
+int row_inv_norms(const Op<T> &op, bool adj, T *rinv, cudaStream_t st);
+int pick_tile_shape(int nx, int ny, int nz);
+int num_tile_shapes();
 
 // h3d_block.cu: the BLOCK ordering (block wavefront, 27 colours inside a block).
 template <typename T>

@@ -1,0 +1,207 @@
+// Matrix-free matvec y = H x (and H^H x, dH x, dH^H x) as a z-marching stencil.
+//
+// A CTA owns a 32 x 8 column of rows and marches a chunk of planes in z.  Each plane of
+// x (and, forward, of the wavenumber) is staged in shared memory with its one-point xy
+// halo by asynchronous copies (double-buffered: plane p+1 streams in while plane p is
+// used).  From a plane every thread forms the partial sums of its 3 x 3 in-plane
+// neighbourhood that the stencil needs -- centre, the two x-faces, the two y-faces and
+// the corner pairs grouped by the sign of dx and of dy -- and keeps the last three planes
+// in registers (a register queue along z).  One output row then combines planes k-1,
+// k, k+1 with its own PML values: the 27 coefficients of Helm3d_27pt.h:676-825 regroup
+// into 9 complex factors (xi_lo / xi_hi per axis and the per-axis sums S) multiplying
+// real-weighted brackets of plane sums, plus the wavenumber (mass) part.  The adjoint
+// uses the same algebra with the neighbour-shifted, conjugated PML values and the
+// centre wavenumber; the derivative variants keep only the mass part.
+//
+// The same kernel produces the FP64 residual r = b - A x with per-block partial sums of
+// ||r||^2 and ||b||^2 (RESID).
+#include "h3d_internal.cuh"
+#include "h3d_kernels.cuh"
+#include "h3d_reduce.cuh"
+#include "h3d_planes.cuh"
+
+namespace h3d {
+
+constexpr int kMX = 32, kMY = 8;                 // CTA columns
+constexpr int kPX = kMX + 2, kPY = kMY + 2;      // staged plane with halo
+constexpr int kPN = kPX * kPY;
+
+template <int BYTES>
+__device__ __forceinline__ void mv_cp_async(void *sdst, const void *gsrc, bool valid)
+{
+    const unsigned s = (unsigned)__cvta_generic_to_shared(sdst);
+    const int n = valid ? BYTES : 0;
+    if constexpr (BYTES == 16)
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s), "l"(gsrc), "r"(n) : "memory");
+    else
+        asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gsrc), "n"(BYTES), "r"(n) : "memory");
+}
+
+template <typename T, bool ADJ, bool DERIV, bool WNC, bool RESID>
+__global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cplx<T> *__restrict__ x,
+                                                              cplx<T> *__restrict__ y,
+                                                              const cplx<T> *__restrict__ b, int kz,
+                                                              int nchunks, double *part)
+{
+    constexpr bool NEED_WN = !ADJ;  // forward: neighbour wavenumbers; adjoint: centre only
+    __shared__ __align__(16) cplx<T> sx[2][kPN];
+    __shared__ T swr[NEED_WN ? 2 : 1][NEED_WN ? kPN : 1];
+    __shared__ T swi[NEED_WN && WNC ? 2 : 1][NEED_WN && WNC ? kPN : 1];
+
+    const int tid = threadIdx.x + kMX * threadIdx.y;
+    const int s = blockIdx.z / nchunks, chunk = blockIdx.z % nchunks;
+    const int kb = chunk * kz, ke = min(op.nz, kb + kz);
+    const int i0 = blockIdx.x * kMX, j0 = blockIdx.y * kMY;
+    const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
+    const bool valid = i < op.nx && j < op.ny;
+    const cplx<T> *xs = x + (long long)s * op.N;
+
+    auto stage = [&](int buf, int pk) {
+        const bool kin = pk >= 0 && pk < op.nz;
+        for (int e = tid; e < kPN; e += kMX * kMY) {
+            const int li = e % kPX, lj = e / kPX;
+            const int gi = i0 - 1 + li, gj = j0 - 1 + lj;
+            const bool in = kin && gi >= 0 && gi < op.nx && gj >= 0 && gj < op.ny;
+            const long long g = in ? gi + op.sy * gj + op.sz * pk : 0;
+            mv_cp_async<sizeof(cplx<T>)>(&sx[buf][e], xs + g, in);
+            if constexpr (NEED_WN) {
+                mv_cp_async<sizeof(T)>(&swr[buf][e], op.wn + g, in);
+                if constexpr (WNC) mv_cp_async<sizeof(T)>(&swi[buf][e], op.wni + g, in);
+            }
+        }
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+    };
+
+    RowPml<T> pml{};
+    if (valid && !DERIV) pml = load_row_pml<T, ADJ>(op, i, j, 0);
+    const int l = (threadIdx.x + 1) + kPX * (threadIdx.y + 1);
+    // Register queue: brackets of the rows pk-1 (A0), pk (A1) and pk+1 (A2) while plane pk
+    // is staged; plane pk completes row pk-1.
+    RowAcc<T> A0, A1, A2;
+    acc_zero(A0);
+    acc_zero(A1);
+    acc_zero(A2);
+    double rr = 0.0, bb = 0.0;
+
+    stage(0, kb - 1);
+    for (int pk = kb - 1; pk <= ke; ++pk) {
+        const int buf = (pk - (kb - 1)) & 1;
+        if (pk + 1 <= ke) {
+            stage(buf ^ 1, pk + 1);
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");
+        } else {
+            asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+        }
+        __syncthreads();
+        {
+            const PlaneSums<T> P = plane_sums<T, ADJ, WNC, kPX>(sx[buf], NEED_WN ? swr[buf] : nullptr,
+                                                                NEED_WN && WNC ? swi[buf] : nullptr, l);
+            acc_plane<2, T, DERIV>(A0, P, op);
+            acc_plane<1, T, DERIV>(A1, P, op);
+            acc_plane<0, T, DERIV>(A2, P, op);
+        }
+        __syncthreads();
+        const int k = pk - 1;  // row completed by this plane
+        if (k >= kb && valid) {
+            RowPml<T> p = pml;
+            if constexpr (!DERIV) {
+                // only the z values change along the march
+                const cplx<T> *t = op.tab;
+                p.Sz = t[op.sum[2] + k + 1];
+                if constexpr (!ADJ) {
+                    p.Azm = t[op.lo[2] + k + 1];
+                    p.Azp = t[op.hi[2] + k + 1];
+                } else {
+                    p.Azm = t[op.hi[2] + k];
+                    p.Azp = t[op.lo[2] + k + 2];
+                }
+            }
+            const long long ctr = i + op.sy * j + op.sz * k;
+            cplx<T> wc = mk<T>(T(0), T(0));
+            if constexpr (ADJ) wc = load_wn<T, WNC>(op, ctr);
+            const cplx<T> v = acc_finish<T, ADJ, DERIV, WNC>(A0, p, wc);
+            if constexpr (RESID) {
+                const cplx<T> bv = b[(long long)s * op.N + ctr];
+                const cplx<T> r = bv - v;
+                y[(long long)s * op.N + ctr] = r;
+                rr += (double)cabs2(r);
+                bb += (double)cabs2(bv);
+            } else {
+                y[(long long)s * op.N + ctr] = v;
+            }
+        }
+        A0 = A1;
+        A1 = A2;
+        acc_zero(A2);
+    }
+    if constexpr (RESID) {
+        const double2 t = block_sum2_r(rr, bb);
+        if (tid == 0) {
+            const long long G = (long long)gridDim.x * gridDim.y * nchunks;
+            const long long blin = blockIdx.x + gridDim.x * (blockIdx.y + (long long)gridDim.y * chunk);
+            part[2 * (s * G + blin)] = t.x;
+            part[2 * (s * G + blin) + 1] = t.y;
+        }
+    }
+}
+
+static int chunk_len(int nz) { return nz < 32 ? nz : 16; }
+
+template <typename T>
+static dim3 zmarch_grid(const Op<T> &op, int nrhs, int *kz, int *nchunks)
+{
+    *kz = chunk_len(op.nz);
+    *nchunks = (op.nz + *kz - 1) / *kz;
+    return dim3((op.nx + kMX - 1) / kMX, (op.ny + kMY - 1) / kMY, *nchunks * nrhs);
+}
+
+template <typename T, bool RESID>
+static int zmarch_dispatch(const Op<T> &op, const cplx<T> *x, cplx<T> *y, const cplx<T> *b, int nrhs,
+                           bool adj, bool deriv, double *part, cudaStream_t st)
+{
+    int kz, nch;
+    const dim3 grd = zmarch_grid(op, nrhs, &kz, &nch);
+    if ((long long)nch * nrhs > 65535) {
+        set_error("too many right-hand sides for one launch");
+        return H3D_ERR_BAD_ARG;
+    }
+    const dim3 blk(kMX, kMY);
+    const bool wnc = op.wni != nullptr;
+#define H3D_ZM(A, D, W) mvp_zmarch_kernel<T, A, D, W, RESID><<<grd, blk, 0, st>>>(op, x, y, b, kz, nch, part)
+    if (!adj && !deriv && !wnc) H3D_ZM(false, false, false);
+    else if (!adj && !deriv && wnc) H3D_ZM(false, false, true);
+    else if (!adj && deriv && !wnc) H3D_ZM(false, true, false);
+    else if (!adj && deriv && wnc) H3D_ZM(false, true, true);
+    else if (adj && !deriv && !wnc) H3D_ZM(true, false, false);
+    else if (adj && !deriv && wnc) H3D_ZM(true, false, true);
+    else if (adj && deriv && !wnc) H3D_ZM(true, true, false);
+    else H3D_ZM(true, true, true);
+#undef H3D_ZM
+    H3D_CUDA_TRY(cudaGetLastError());
+    return H3D_OK;
+}
+
+template <typename T>
+int launch_mvp(const Op<T> &op, const cplx<T> *x, cplx<T> *y, int nrhs, bool adj, bool deriv,
+               cudaStream_t st)
+{
+    return zmarch_dispatch<T, false>(op, x, y, nullptr, nrhs, adj, deriv, nullptr, st);
+}
+
+int mvp_residual_parts(const Op<double> &op, int nrhs)
+{
+    int kz, nch;
+    const dim3 g = zmarch_grid(op, nrhs, &kz, &nch);
+    return (int)(g.x * g.y * nch);
+}
+
+int launch_residual(const Op<double> &op, const cplx<double> *b, const cplx<double> *x, cplx<double> *r,
+                    int nrhs, bool adj, double *part, cudaStream_t st)
+{
+    return zmarch_dispatch<double, true>(op, x, r, b, nrhs, adj, false, part, st);
+}
+
+template int launch_mvp<double>(const Op<double> &, const cplx<double> *, cplx<double> *, int, bool, bool, cudaStream_t);
+template int launch_mvp<float>(const Op<float> &, const cplx<float> *, cplx<float> *, int, bool, bool, cudaStream_t);
+
+}  // namespace h3d

@@ -1,0 +1,147 @@
+// Plane-sum form of one row of the 27-point operator, shared by the matvec and the
+// sweep gather.  The coefficients of Helm3d_27pt.h:676-825 regroup per z-plane: from the
+// 3 x 3 in-plane neighbourhood a thread forms the centre, the x- and y-face values and the
+// corner pairs split by the sign of dx and of dy; a row then combines planes k-1, k, k+1
+// into 9 complex PML factors (xi per direction, S per axis) times real-weighted brackets
+// of those sums, plus the wavenumber (mass) part.
+#pragma once
+
+#include "h3d_internal.cuh"
+
+namespace h3d {
+
+// Plane partial sums of one thread.  W* are the mass sums: forward, weighted by the
+// neighbour's wavenumber; adjoint, unweighted (the centre wavenumber multiplies later).
+template <typename T>
+struct PlaneSums {
+    cplx<T> m, fxm, fxp, fym, fyp, cxm, cxp, cym, cyp;  // cxm = corners with dx = -1, ...
+    cplx<T> wm, wfx, wfy, wc4;
+};
+
+template <typename T, bool WNC>
+__device__ __forceinline__ cplx<T> wmul(cplx<T> w, cplx<T> v)
+{
+    if constexpr (WNC) return w * v;
+    else return mk<T>(w.re * v.re, w.re * v.im);
+}
+
+template <typename T, bool ADJ, bool WNC, int PITCH>
+__device__ __forceinline__ PlaneSums<T> plane_sums(const cplx<T> *sxp, const T *swr, const T *swi, int l)
+{
+    // l = index of the thread's centre in the staged plane, PITCH = its row pitch
+    auto X = [&](int dx, int dy) { return sxp[l + dx + PITCH * dy]; };
+    auto W = [&](int dx, int dy) {
+        const int q = l + dx + PITCH * dy;
+        return mk<T>(swr[q], WNC ? swi[q] : T(0));
+    };
+    PlaneSums<T> p;
+    const cplx<T> mm = X(-1, -1), mp = X(-1, 1), pm = X(1, -1), pp = X(1, 1);
+    p.m = X(0, 0);
+    p.fxm = X(-1, 0);
+    p.fxp = X(1, 0);
+    p.fym = X(0, -1);
+    p.fyp = X(0, 1);
+    p.cxm = mm + mp;
+    p.cxp = pm + pp;
+    p.cym = mm + pm;
+    p.cyp = mp + pp;
+    if constexpr (!ADJ) {
+        p.wm = wmul<T, WNC>(W(0, 0), p.m);
+        p.wfx = wmul<T, WNC>(W(-1, 0), p.fxm) + wmul<T, WNC>(W(1, 0), p.fxp);
+        p.wfy = wmul<T, WNC>(W(0, -1), p.fym) + wmul<T, WNC>(W(0, 1), p.fyp);
+        p.wc4 = wmul<T, WNC>(W(-1, -1), mm) + wmul<T, WNC>(W(-1, 1), mp) + wmul<T, WNC>(W(1, -1), pm) +
+                wmul<T, WNC>(W(1, 1), pp);
+    } else {
+        p.wm = p.m;
+        p.wfx = p.fxm + p.fxp;
+        p.wfy = p.fym + p.fyp;
+        p.wc4 = p.cxm + p.cxp;
+    }
+    return p;
+}
+
+template <typename T>
+__device__ __forceinline__ cplx<T> rc(T a, cplx<T> v) { return mk<T>(a * v.re, a * v.im); }
+
+// Brackets of one pending row: the mass part and the real-weighted sums multiplying each
+// of the 9 complex PML factors (xi per direction and axis, S per axis).  Planes are
+// added one at a time in the role they play for the row: L (k-1), C (k) or U (k+1).
+template <typename T>
+struct RowAcc {
+    cplx<T> mass, bxm, bxp, bym, byp, bzm, bzp, bsx, bsy, bsz;
+};
+
+template <typename T>
+__device__ __forceinline__ void acc_zero(RowAcc<T> &a)
+{
+    const cplx<T> z = mk<T>(T(0), T(0));
+    a.mass = a.bxm = a.bxp = a.bym = a.byp = a.bzm = a.bzp = a.bsx = a.bsy = a.bsz = z;
+}
+
+template <typename T>
+__device__ __forceinline__ void fma_rc(cplx<T> &acc, T s, cplx<T> v)
+{
+    acc.re += s * v.re;
+    acc.im += s * v.im;
+}
+
+// ROLE: 0 = the plane below the row (k-1), 1 = the row's plane, 2 = the plane above.
+template <int ROLE, typename T, bool DERIV>
+__device__ __forceinline__ void acc_plane(RowAcc<T> &a, const PlaneSums<T> &P, const Op<T> &op)
+{
+    const T w3 = op.w3a2;
+    if constexpr (ROLE == 1) {
+        fma_rc(a.mass, op.wn_c, P.wm);
+        fma_rc(a.mass, T(-kWM2), P.wfx + P.wfy);
+        fma_rc(a.mass, T(-kWM3), P.wc4);
+    } else {
+        fma_rc(a.mass, T(-kWM2), P.wm);
+        fma_rc(a.mass, T(-kWM3), P.wfx + P.wfy);
+        fma_rc(a.mass, T(-kWM4), P.wc4);
+    }
+    if constexpr (!DERIV) {
+        const cplx<T> fx = P.fxm + P.fxp, fy = P.fym + P.fyp, c4 = P.cxm + P.cxp;
+        if constexpr (ROLE == 1) {
+            fma_rc(a.bxm, op.pml_x, P.fxm); fma_rc(a.bxm, -op.xy, P.cxm);
+            fma_rc(a.bxp, op.pml_x, P.fxp); fma_rc(a.bxp, -op.xy, P.cxp);
+            fma_rc(a.bym, op.pml_y, P.fym); fma_rc(a.bym, -op.xy, P.cym);
+            fma_rc(a.byp, op.pml_y, P.fyp); fma_rc(a.byp, -op.xy, P.cyp);
+            fma_rc(a.bsx, op.wn_x, P.m); fma_rc(a.bsx, op.xy, fy);
+            fma_rc(a.bsy, op.wn_y, P.m); fma_rc(a.bsy, op.xy, fx);
+            fma_rc(a.bsz, op.wn_z, P.m); fma_rc(a.bsz, op.xz, fx); fma_rc(a.bsz, op.yz, fy); fma_rc(a.bsz, w3, c4);
+        } else {
+            fma_rc(a.bxm, -op.xz, P.fxm); fma_rc(a.bxm, -w3, P.cxm);
+            fma_rc(a.bxp, -op.xz, P.fxp); fma_rc(a.bxp, -w3, P.cxp);
+            fma_rc(a.bym, -op.yz, P.fym); fma_rc(a.bym, -w3, P.cym);
+            fma_rc(a.byp, -op.yz, P.fyp); fma_rc(a.byp, -w3, P.cyp);
+            fma_rc(a.bsx, op.xz, P.m); fma_rc(a.bsx, w3, fy);
+            fma_rc(a.bsy, op.yz, P.m); fma_rc(a.bsy, w3, fx);
+            cplx<T> &bz = ROLE == 0 ? a.bzm : a.bzp;
+            fma_rc(bz, op.pml_z, P.m); fma_rc(bz, -op.xz, fx); fma_rc(bz, -op.yz, fy); fma_rc(bz, -w3, c4);
+        }
+    }
+}
+
+// y = (adjoint: conj(wn_centre) *) mass + sum over the 9 factors of factor * bracket
+// (adjoint: the conjugated, neighbour-shifted factors).
+template <typename T, bool ADJ, bool DERIV, bool WNC>
+__device__ __forceinline__ cplx<T> acc_finish(const RowAcc<T> &a, const RowPml<T> &p, cplx<T> wc)
+{
+    cplx<T> y = a.mass;
+    if constexpr (ADJ) y = WNC ? cconj(wc) * y : mk<T>(wc.re * y.re, wc.re * y.im);
+    if constexpr (!DERIV) {
+        auto f = [&](cplx<T> v) { return ADJ ? cconj(v) : v; };
+        cmac(y, f(p.Axm), a.bxm);
+        cmac(y, f(p.Axp), a.bxp);
+        cmac(y, f(p.Aym), a.bym);
+        cmac(y, f(p.Ayp), a.byp);
+        cmac(y, f(p.Azm), a.bzm);
+        cmac(y, f(p.Azp), a.bzp);
+        cmac(y, f(p.Sx), a.bsx);
+        cmac(y, f(p.Sy), a.bsy);
+        cmac(y, f(p.Sz), a.bsz);
+    }
+    return y;
+}
+
+}  // namespace h3d

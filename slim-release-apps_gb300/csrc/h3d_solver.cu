@@ -9,6 +9,9 @@
 // replayed; per-RHS masks freeze converged right-hand sides on the device, and the host
 // only reads the mask every check_every iterations.
 #include <chrono>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -22,50 +25,8 @@
 
 namespace h3d {
 
-// ---------------------------------------------------------------------------------------
-// FP64 residual r = b - A x, fused with the per-block partial sums of ||r||^2 and ||b||^2.
-template <bool ADJ, bool WNC>
-__global__ void __launch_bounds__(256) residual_kernel(Op<double> op, const cplx<double> *__restrict__ b,
-                                                       const cplx<double> *__restrict__ x,
-                                                       cplx<double> *__restrict__ r, int nrhs,
-                                                       double *part, int G)
-{
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y;
-    const int k = blockIdx.z;
-    const bool valid = i < op.nx && j < op.ny;
-    const int blin = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
-    cplx<double> c[27];
-    uint32_t m = 0;
-    long long ctr = 0;
-    if (valid) {
-        m = inside_mask(i, j, k, op.nx, op.ny, op.nz);
-        row_coefs<double, ADJ, false, WNC>(op, i, j, k, m, c);
-        ctr = i + op.sy * j + op.sz * k;
-    }
-    for (int s = 0; s < nrhs; ++s) {
-        double rr = 0.0, bb = 0.0;
-        if (valid) {
-            const cplx<double> *xs = x + (long long)s * op.N + ctr;
-            cplx<double> acc = mk(0.0, 0.0);
-#define H3D_ACC(t, dx, dy, dz) \
-    if (m & (1u << t)) cmac(acc, c[t], xs[dx + op.sy * dy + op.sz * dz]);
-            H3D_FOR_27(H3D_ACC)
-#undef H3D_ACC
-            const cplx<double> bv = b[(long long)s * op.N + ctr];
-            const cplx<double> rv = bv - acc;
-            r[(long long)s * op.N + ctr] = rv;
-            rr = cabs2(rv);
-            bb = cabs2(bv);
-        }
-        const double2 t = block_sum2_r(rr, bb);
-        if (threadIdx.x == 0 && threadIdx.y == 0) {
-            part[2 * ((long long)s * G + blin)] = t.x;
-            part[2 * ((long long)s * G + blin) + 1] = t.y;
-        }
-    }
-}
-
+// FP64 residual r = b - A x (z-marching matvec kernel with fused norms), then one block
+// per right-hand side sums the per-block partials in a fixed order.
 __global__ void residual_reduce(const double *part, int G, double *rr2, double *bb2)
 {
     const int s = blockIdx.x;
@@ -81,27 +42,36 @@ __global__ void residual_reduce(const double *part, int G, double *rr2, double *
     }
 }
 
-static dim3 residual_grid(const Op<double> &op) { return dim3((op.nx + 31) / 32, (op.ny + 7) / 8, op.nz); }
-
 int residual_f64(const Op<double> &op, const cplx<double> *b, const cplx<double> *x,
                  cplx<double> *r, double *rr2, double *bb2, int nrhs, bool adj, double *part,
                  int G, cudaStream_t st)
 {
-    const dim3 grd = residual_grid(op), blk(32, 8);
-    const bool wnc = op.wni != nullptr;
-    if (!adj && !wnc) residual_kernel<false, false><<<grd, blk, 0, st>>>(op, b, x, r, nrhs, part, G);
-    else if (!adj && wnc) residual_kernel<false, true><<<grd, blk, 0, st>>>(op, b, x, r, nrhs, part, G);
-    else if (adj && !wnc) residual_kernel<true, false><<<grd, blk, 0, st>>>(op, b, x, r, nrhs, part, G);
-    else residual_kernel<true, true><<<grd, blk, 0, st>>>(op, b, x, r, nrhs, part, G);
+    int rc = launch_residual(op, b, x, r, nrhs, adj, part, st);
+    if (rc) return rc;
     residual_reduce<<<nrhs, 256, 0, st>>>(part, G, rr2, bb2);
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;
 }
 
-static int residual_parts(const Op<double> &op)
+// ---------------------------------------------------------------------------------------
+// Autotuner cache: (nx, ny, nz, element size, adjoint, complex wn, nrhs) -> tile shape.
+using TuneKey = std::tuple<int, int, int, int, int, int, int>;
+static std::mutex g_tune_mutex;
+static std::map<TuneKey, int> g_tune_cache;
+
+static bool tune_lookup(const TuneKey &k, int *shape)
 {
-    const dim3 g = residual_grid(op);
-    return (int)(g.x * g.y * g.z);
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    auto it = g_tune_cache.find(k);
+    if (it == g_tune_cache.end()) return false;
+    *shape = it->second;
+    return true;
+}
+
+static void tune_store(const TuneKey &k, int shape)
+{
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    g_tune_cache[k] = shape;
 }
 
 // ---------------------------------------------------------------------------------------
@@ -117,8 +87,10 @@ struct CgRun {
     int32_t block[3] = {0, 0, 0};
     int maxit = 10000;
     cplx<T> *x = nullptr, *r = nullptr, *p = nullptr, *y = nullptr;
+    T *rinv = nullptr;   // 1/||a_i||^2 per row, computed once (COLOUR27)
+    int shape = -1;      // COLOUR27 tile shape
     CgState s{};
-    DevBuf vecs, scal, ints, parts;
+    DevBuf vecs, scal, ints, parts, norms;
     cudaGraphExec_t exec = nullptr;
     int graph_iters = 0;
     // Timing of the last double sweep of every replayed block: two timing events recorded
@@ -177,6 +149,12 @@ struct CgRun {
         s.status = q + 3 * nrhs;
         if ((rc = parts.alloc(sizeof(double) * 2 * (size_t)s.G * nrhs, st))) return rc;
         s.part = parts.as<double>();
+        if (order == H3D_ORDER_COLOUR27) {
+            if ((rc = norms.alloc(sizeof(T) * (size_t)N, st))) return rc;
+            rinv = norms.as<T>();
+            if ((rc = row_inv_norms<T>(op, adj, rinv, st))) return rc;
+            ++launches;
+        }
         return H3D_OK;
     }
 
@@ -197,12 +175,50 @@ struct CgRun {
         return 2 * n;
     }
 
+    // Tile-shape autotuner for the COLOUR27 sweep: time one double sweep per candidate
+    // shape on the scratch vector y (its contents are overwritten by setup right after)
+    // and keep the fastest; decisions are cached per (grid, precision, mode, nrhs).
+    int tune(cudaStream_t st)
+    {
+        if (order != H3D_ORDER_COLOUR27 || shape >= 0) return H3D_OK;
+        const TuneKey key{op.nx, op.ny, op.nz, (int)sizeof(T), adj ? 1 : 0, op.wni ? 1 : 0, nrhs};
+        if (tune_lookup(key, &shape)) return H3D_OK;
+        cudaEvent_t e0, e1;
+        H3D_CUDA_TRY(cudaEventCreate(&e0));
+        H3D_CUDA_TRY(cudaEventCreate(&e1));
+        float best = 1e30f;
+        int best_shape = 0;
+        int rc = zero_vec<T>(y, N, nrhs, st);
+        for (int sh = 0; sh < num_tile_shapes() && !rc; ++sh) {
+            if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, nullptr, st, rinv, sh))) break;
+            cudaEventRecord(e0, st);
+            for (int rep = 0; rep < 2 && !rc; ++rep)
+                rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, nullptr, st, rinv, sh);
+            cudaEventRecord(e1, st);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best) {
+                best = ms;
+                best_shape = sh;
+            }
+            launches += 3LL * sweep_launches();
+        }
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        if (rc) return rc;
+        shape = best_shape;
+        tune_store(key, shape);
+        return H3D_OK;
+    }
+
     // b~ = DSWP(0, b) into y, then x = 0, r = p = y.
     int setup(const cplx<T> *b, const double *bnorm2_orig, double zero_tol2, cudaStream_t st)
     {
         int rc;
+        if ((rc = tune(st))) return rc;
         if ((rc = zero_vec<T>(y, N, nrhs, st))) return rc;
-        if ((rc = launch_sweep<T>(op, y, b, nrhs, w, adj, order, block, nullptr, st))) return rc;
+        if ((rc = launch_sweep<T>(op, y, b, nrhs, w, adj, order, block, nullptr, st, rinv, shape))) return rc;
         launches += sweep_launches() + 2;
         return cg_init<T>(y, x, r, p, N, nrhs, s, bnorm2_orig, zero_tol2, maxit, st);
     }
@@ -211,7 +227,7 @@ struct CgRun {
     {
         int rc;
         if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev0, st, cudaEventRecordExternal));
-        if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st))) return rc;
+        if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st, rinv, shape))) return rc;
         if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev1, st, cudaEventRecordExternal));
         if ((rc = cg_ap_dot<T>(p, y, N, nrhs, s, st))) return rc;
         if ((rc = cg_update_xr<T>(x, r, p, y, N, nrhs, s, maxit, st))) return rc;
@@ -352,7 +368,7 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
     const double zero_tol2 = 1e-24;  // (1e-12)^2, opAbstractMatrix.m:118
 
     // FP64 residual machinery: r64 = b - A u, per-RHS norms.
-    const int Gr = residual_parts(op64);
+    const int Gr = mvp_residual_parts(op64, nrhs);
     DevBuf r64b, partb, normb;
     if ((rc = r64b.alloc(sizeof(cplx<double>) * (size_t)N * nrhs, st))) return rc;
     if ((rc = partb.alloc(sizeof(double) * 2 * (size_t)Gr * nrhs, st))) return rc;
@@ -583,7 +599,7 @@ int h3d_residual(const h3d_grid *g, const double *wn_re, const double *wn_im, co
     int rc = make_op_f64(g, wn_re, wn_im, &op);
     if (rc) return rc;
     cudaStream_t st = (cudaStream_t)stream;
-    const int G = residual_parts(op);
+    const int G = mvp_residual_parts(op, nrhs);
     DevBuf part, norms;
     if ((rc = part.alloc(sizeof(double) * 2 * (size_t)G * nrhs, st))) return rc;
     if ((rc = norms.alloc(sizeof(double) * 2 * (size_t)nrhs, st))) return rc;

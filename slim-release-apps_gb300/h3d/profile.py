@@ -21,7 +21,7 @@ from . import models, ops
 
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--kernel", choices=["sweep", "mvp", "mvp_adj"], default="sweep")
+    ap.add_argument("--kernel", choices=["sweep", "mvp", "mvp_adj", "cgmn"], default="sweep")
     ap.add_argument("--config", type=int, choices=[0, 1], default=1)
     ap.add_argument("--dtype", choices=["c64", "c128"], default="c64")
     ap.add_argument("--order", type=int, default=L.ORDER_COLOUR27)
@@ -36,7 +36,16 @@ def main(argv=None):
     wn = torch.as_tensor(m.wavenumber(), device=dev).to(rdt)
     gen = torch.Generator(device=dev).manual_seed(0)
     x = torch.randn(a.nrhs, m.N, dtype=cdt, device=dev, generator=gen)
-    if a.kernel == "sweep":
+    if a.kernel == "cgmn":
+        # a fixed number of CGMN iterations of the solver (sweeps with precomputed norms)
+        from . import solver
+
+        b = torch.as_tensor(m.point_source(), device=dev)
+        opts = solver.make_opts(tol=1e-30, maxit=a.reps, precision="fp64" if a.dtype == "c128" else "mixed",
+                                order=a.order, max_outer=1, inner_tol=1e-30, check_every=a.reps)
+        fn = lambda: solver.solve(grid, wn.double(), b, opts=opts, raise_not_converged=False)
+        bytes_per = a.reps * 2 * m.N * (2 * (8 if a.dtype == "c64" else 16) + (4 if a.dtype == "c64" else 8))
+    elif a.kernel == "sweep":
         fn = lambda: ops.kacz_sweep(grid, wn, 1.5, x, None, 1, order=a.order, block=a.block)
         bytes_per = 2 * m.N * (2 * (8 if a.dtype == "c64" else 16) * a.nrhs + (4 if a.dtype == "c64" else 8))
     else:
@@ -45,6 +54,8 @@ def main(argv=None):
         bytes_per = m.N * (2 * (8 if a.dtype == "c64" else 16) * a.nrhs + (4 if a.dtype == "c64" else 8))
     fn()
     torch.cuda.synchronize()
+    if a.kernel == "cgmn":
+        a.reps = 1
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record()
     for _ in range(a.reps):
