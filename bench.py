@@ -44,9 +44,11 @@ WORKLOAD = "config1: 201x201x101 incl. 20-pt PML, h=20 m, 6 Hz, single surface s
 
 # CGMN iterations the reference ordering (lexicographic Kaczmarz double sweep,
 # linearsolve.m:148-156 + CGMN.m) needs on this workload to reach a true relative
-# residual of 1e-6, measured with the library's LEX path (identical arithmetic to the
-# reference sweep); used to extrapolate the CPU per-iteration time to a solve.
-REF_ITERS_CONFIG1 = None  # filled from a measured run; see --measure-ref-iters
+# residual of 1e-6 (true residual 5.08e-7 at stop), measured on a GB300 with the
+# library's LEX path, whose arithmetic is the reference sweep's (h3d_solve, order LEX,
+# precision FP64, stop on the true residual; 148 s).  The CPU per-iteration time
+# measured here times this count is the extrapolated CPU solve time.
+REF_ITERS_CONFIG1 = 1481
 
 
 def _peaks():

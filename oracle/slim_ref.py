@@ -254,7 +254,8 @@ def pdefunc(func, v_phys, model, src_pts, src_amp, rec_pts, freqs, Dobs=None, to
         for s in range(nsrc):                                                        # :324
             q = inject(n_total, axes, [src_pts[s]], [w[k] * src_amp[s]])[:, 0]       # :335
             q = q * np.prod(d) / np.prod(d)                                          # :339
-            U = cgmn_solve(g, wn, q, tol=tol, maxit=maxit, order=order)              # :347
+            U = divide(g, wn, q, mode=1, tol=tol, maxit=maxit, order=order,
+                       nthreads=nthreads)[0]                                         # :347
             dpred = sample(n_total, axes, rec_pts, U)[:, 0]
             if func == "forw_model":
                 out[:, col] = dpred                                                  # :423
@@ -262,7 +263,8 @@ def pdefunc(func, v_phys, model, src_pts, src_amp, rec_pts, freqs, Dobs=None, to
                 phi, dphi = ls_misfit(dpred, Dobs[:, col])                           # :389
                 f += phi
                 rhs = -spread(n_total, axes, rec_pts, dphi)[:, 0]
-                V = cgmn_solve(g, wn, rhs, tol=tol, maxit=maxit, mode=2, order=order)  # :393
+                V = divide(g, wn, rhs, mode=2, tol=tol, maxit=maxit, order=order,
+                           nthreads=nthreads)[0]                                     # :393
                 # T(U)'*V = conj(U) .* (dH' * V)  (dh:288), real part, to_phys = crop (dh:232)
                 dHV = O.mvp(g, dwn, V, adj=True, deriv=True, nthreads=nthreads)
                 tu = np.real(np.conj(U) * dHV).reshape(n_total, order="F")
