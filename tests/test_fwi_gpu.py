@@ -81,7 +81,7 @@ def test_taylor_second_order(cuda):
     rng = np.random.default_rng(3)
     dm = np.zeros(geom.n)
     dm[1:-1, 1:-1, 1:-1] = rng.standard_normal((geom.n[0] - 2, geom.n[1] - 2, geom.n[2] - 2))
-    dm *= 0.05 * np.abs(m0).max() / np.abs(dm).max()
+    dm *= 0.002 * np.abs(m0).max() / np.abs(dm).max()
     f0, g = prob.objective(torch.as_tensor(m0, device=cuda), Dobs)
     gdm = float(torch.sum(g * torch.as_tensor(dm, device=cuda)))
     hs = [2.0 ** -k for k in range(6)]
