@@ -156,6 +156,21 @@ int h3d_residual(const h3d_grid *g, const double *wn_re, const double *wn_im, co
                  const void *x, void *r, double *rr2, double *bb2, int nrhs, int mode,
                  void *stream);
 
+/* Same result as h3d_residual, for callers that cannot allocate device memory: code whose
+ * device memory is owned by its own allocator or fixed budget (a library-side allocation
+ * would fail there or break the caller's accounting).  No counterpart in the reference.
+ * All scratch (the PML tables and the per-block partial sums) lives in one fixed device
+ * array of H3D_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until the
+ * process exits; grids and nrhs needing more are rejected with H3D_ERR_BAD_ARG.  The
+ * first call on a device looks up that array's address (once per device, with the device
+ * current); make the first call before any stream capture.  Every call reuses the same
+ * array, so calls that overlap on the GPU (other streams, other threads) race: serialise
+ * them.  Each call rewrites all the scratch it reads, so no state carries over. */
+#define H3D_NOALLOC_SCRATCH_BYTES (4u << 20)
+int h3d_residual_noalloc(const h3d_grid *g, const double *wn_re, const double *wn_im,
+                         const void *b, const void *x, void *r, double *rr2, double *bb2,
+                         int nrhs, int mode, void *stream);
+
 /* ---- MATLAB-layout host entry points (what the drop-in MEX gateway calls) ----------- */
 /* Arguments exactly as the reference gateways receive them: wn (N, re/im planes; im may
  * be NULL), h[3], n[3] and npml[6] as doubles, x split into re/im planes (im may be

@@ -244,6 +244,50 @@ int make_op_f64(const h3d_grid *g, const double *wn, const double *wni, Op<doubl
     return make_op<double>(g, wn, wni, op);
 }
 
+// FP64 operator whose PML tables live at a caller-chosen device address (no allocation,
+// no table cache): the host tables are returned in *host_tab for the caller to copy to
+// dev_tab.  Used by the entry point that must not allocate device memory.
+int make_op_f64_at(const h3d_grid *g, const double *wn, const double *wni, const void *dev_tab,
+                   std::vector<cplx<double>> *host_tab, Op<double> *op)
+{
+    int rc = check_grid(g);
+    if (rc) return rc;
+    std::vector<std::complex<double>> tab;
+    Op<double> o{};
+    fill_tables(g, tab, o.lo, o.hi, o.sum);
+    host_tab->resize(tab.size());
+    for (size_t q = 0; q < tab.size(); ++q) (*host_tab)[q] = mk<double>(tab[q].real(), tab[q].imag());
+    o.nx = g->n[0];
+    o.ny = g->n[1];
+    o.nz = g->n[2];
+    o.sy = o.nx;
+    o.sz = (long long)o.nx * o.ny;
+    o.N = o.sz * o.nz;
+    o.wn = wn;
+    o.wni = wni;
+    o.tab = (const cplx<double> *)dev_tab;
+    const double hx2 = g->h[0] * g->h[0], hy2 = g->h[1] * g->h[1], hz2 = g->h[2] * g->h[2];
+    const double hxy = hx2 + hy2, hxz = hx2 + hz2, hyz = hy2 + hz2, hxyz = hx2 + hy2 + hz2;
+    const double w3a = kW3 * 3 / (4 * hxyz);
+    o.w3a2 = 2 * w3a;
+    o.wn_c = -(kW1 + 3 * kW2 + 16 * w3a * hxyz / 3 + kWM1 - 1);
+    o.wn_x = kW1 / hx2 + kW2 / hx2 + kW2 / hxz + kW2 / hxy + 8 * w3a;
+    o.wn_y = kW1 / hy2 + kW2 / hy2 + kW2 / hyz + kW2 / hxy + 8 * w3a;
+    o.wn_z = kW1 / hz2 + kW2 / hz2 + kW2 / hxz + kW2 / hyz + 8 * w3a;
+    o.pml_x = -o.wn_x;
+    o.pml_y = -o.wn_y;
+    o.pml_z = -o.wn_z;
+    o.xz = kW2 / (2 * hxz);
+    o.xy = kW2 / (2 * hxy);
+    o.yz = kW2 / (2 * hyz);
+    // The residual kernel uses only the general coefficient form: no interior fast path.
+    for (int a = 0; a < 3; ++a) {
+        o.int_lo_f[a] = o.int_hi_f[a] = o.int_lo_a[a] = o.int_hi_a[a] = 0;
+    }
+    *op = o;
+    return H3D_OK;
+}
+
 int make_op_f32(const h3d_grid *g, const float *wn, const float *wni, Op<float> *op)
 {
     return make_op<float>(g, wn, wni, op);

@@ -6,6 +6,7 @@
 #include <cuda_runtime.h>
 
 #include <cstdint>
+#include <vector>
 
 #include "h3d.h"
 
@@ -258,6 +259,8 @@ struct DeviceTables;
 
 int make_op_f64(const h3d_grid *g, const double *wn, const double *wni, Op<double> *op);
 int make_op_f32(const h3d_grid *g, const float *wn, const float *wni, Op<float> *op);
+int make_op_f64_at(const h3d_grid *g, const double *wn, const double *wni, const void *dev_tab,
+                   std::vector<cplx<double>> *host_tab, Op<double> *op);
 int check_grid(const h3d_grid *g);
 void set_error(const char *fmt, ...);
 int cuda_fail(cudaError_t e, const char *what);

@@ -1,0 +1,67 @@
+"""h3d_residual_noalloc: the residual entry point for callers that cannot allocate device
+memory (their device memory belongs to their own allocator or to a fixed budget).
+
+Collected last on purpose.  Through the C ABI it must give the same r = b - H x and the
+same per-column ||r||^2 and ||b||^2 as h3d_residual (tolerance 1e-13 relative, the FP64
+matvec tolerance of the other tests), on two calls in a row with different inputs (the
+shared scratch keeps the previous call's contents, which must not leak into the next),
+and it must refuse a problem larger than its fixed scratch with H3D_ERR_BAD_ARG.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _call(fn, grid, wn, b, x, mode):
+    import torch
+    from h3d import _lib as L
+
+    P = b.shape[0]
+    r = torch.empty_like(b)
+    rr = torch.empty(P, dtype=torch.float64, device=b.device)
+    bb = torch.empty(P, dtype=torch.float64, device=b.device)
+    rc = fn(C.byref(grid), C.c_void_p(wn.data_ptr()), C.c_void_p(), C.c_void_p(b.data_ptr()),
+            C.c_void_p(x.data_ptr()), C.c_void_p(r.data_ptr()), C.c_void_p(rr.data_ptr()),
+            C.c_void_p(bb.data_ptr()), P, mode, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return rc, r, rr, bb
+
+
+def test_noalloc_residual_matches_allocating_entry_point(cuda):
+    import torch
+    from h3d import _lib as L
+
+    lib = L.load()
+    n = (30, 28, 26)
+    grid = L.make_grid(n, (25.0, 20.0, 25.0), (5, 4, 5, 5, 3, 5))
+    N = int(np.prod(n))
+    gen = torch.Generator(device=cuda).manual_seed(11)
+    wn = (2 * np.pi * 4.0) ** 2 / (1500 + 2000 * torch.rand(N, dtype=torch.float64, device=cuda, generator=gen)) ** 2
+    for call, (P, mode) in enumerate([(3, L.FORWARD), (2, L.ADJOINT)]):
+        b = torch.randn(P, N, dtype=torch.complex128, device=cuda, generator=gen)
+        x = torch.randn(P, N, dtype=torch.complex128, device=cuda, generator=gen)
+        rc0, r0, rr0, bb0 = _call(lib.h3d_residual, grid, wn, b, x, mode)
+        rc1, r1, rr1, bb1 = _call(lib.h3d_residual_noalloc, grid, wn, b, x, mode)
+        torch.cuda.synchronize()
+        assert rc0 == 0 and rc1 == 0, (call, lib.h3d_last_error())
+        assert ((r1 - r0).abs().max() / r0.abs().max()).item() <= 1e-13
+        assert ((rr1 - rr0).abs() / rr0).max().item() <= 1e-13
+        assert ((bb1 - bb0).abs() / bb0).max().item() <= 1e-13
+
+
+def test_noalloc_residual_rejects_problems_beyond_its_scratch(cuda):
+    import torch
+    from h3d import _lib as L
+
+    lib = L.load()
+    n = (400, 400, 400)            # needs far more partial sums than the fixed scratch holds
+    grid = L.make_grid(n, (10.0, 10.0, 10.0), 10)
+    dummy = torch.zeros(8, dtype=torch.complex128, device=cuda)
+    rc = lib.h3d_residual_noalloc(C.byref(grid), C.c_void_p(dummy.data_ptr()), C.c_void_p(),
+                                  C.c_void_p(dummy.data_ptr()), C.c_void_p(dummy.data_ptr()),
+                                  C.c_void_p(dummy.data_ptr()), C.c_void_p(), C.c_void_p(), 64,
+                                  L.FORWARD, C.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert rc == L.ERR_BAD_ARG
+    assert b"scratch" in lib.h3d_last_error()
