@@ -262,6 +262,54 @@ class FWIProblem:
         g = self.gradient(v_phys, resid, fields)
         return f, _unflat(g, self.geom.n)
 
+    # -- PDEfunc JACOB_FORW / JACOB_ADJ / HESS_GN (PDEfunc.m:426-443) ------------------------------
+    def _born_source(self, dwn, dm_pml, U):
+        """-T(U) dm = -dH diag(dm) U with the forward derivative stencil (discrete_helmholtz.m:287)."""
+        from . import ops
+
+        return -ops.mvp(self.g, dwn, (dm_pml[None, :] * U).contiguous(), 1, deriv=True)
+
+    def jacob_forw(self, v_phys: torch.Tensor, dm_phys: torch.Tensor) -> torch.Tensor:
+        """Born data J dm: dU = H \\ (-T(U) dm), D = Pr dU (PDEfunc.m:426-429); dm is extended
+        into the PML like the model (to_comp = Pext, discrete_helmholtz.m:230)."""
+        dm_pml = _flat(extend_edges(dm_phys.to(self.dev, torch.float64), self.geom.npml6)).to(torch.complex128)
+        cols = []
+        for k, fr in enumerate(self.geom.freqs):
+            wn, dwn = self._wavenumbers(v_phys, float(fr))
+            for srcs in self._batches():
+                U = self._solve(wn, self._sources(k, srcs), 1)
+                dU = self._solve(wn, self._born_source(dwn, dm_pml, U), 1)
+                cols.append(self._sample(dU))
+        return torch.cat(cols, 0).T.contiguous()
+
+    def jacob_adj(self, v_phys: torch.Tensor, dD: torch.Tensor) -> torch.Tensor:
+        """Migration J' dD: V = H' \\ (-Pr' dD), g += crop(Re(conj(U) .* (dH' V))) (PDEfunc.m:431-433)."""
+        g = torch.zeros(int(np.prod(self.geom.n)), dtype=torch.float64, device=self.dev)
+        col = 0
+        for k, fr in enumerate(self.geom.freqs):
+            wn, dwn = self._wavenumbers(v_phys, float(fr))
+            for srcs in self._batches():
+                U = self._solve(wn, self._sources(k, srcs), 1)
+                d = dD[:, col:col + len(srcs)].T.to(torch.complex128)
+                V = self._solve(wn, self._spread(d, -1.0), 2)
+                self._grad_accum(dwn, U, V, g)
+                col += len(srcs)
+        return _unflat(g, self.geom.n)
+
+    def hess_gn(self, v_phys: torch.Tensor, dm_phys: torch.Tensor) -> torch.Tensor:
+        """Gauss-Newton Hessian times dm: per (src,freq) dU = H \\ (-T(U) dm),
+        dU2 = H' \\ (-Pr' Pr dU), g += crop(Re(conj(U) .* (dH' dU2))) (PDEfunc.m:438-442)."""
+        dm_pml = _flat(extend_edges(dm_phys.to(self.dev, torch.float64), self.geom.npml6)).to(torch.complex128)
+        g = torch.zeros(int(np.prod(self.geom.n)), dtype=torch.float64, device=self.dev)
+        for k, fr in enumerate(self.geom.freqs):
+            wn, dwn = self._wavenumbers(v_phys, float(fr))
+            for srcs in self._batches():
+                U = self._solve(wn, self._sources(k, srcs), 1)
+                dU = self._solve(wn, self._born_source(dwn, dm_pml, U), 1)
+                V = self._solve(wn, self._spread(self._sample(dU), -1.0), 2)
+                self._grad_accum(dwn, U, V, g)
+        return _unflat(g, self.geom.n)
+
 
 class FWIObjective(torch.autograd.Function):
     """f(m) with the adjoint-state gradient as its backward.

@@ -115,3 +115,31 @@ def test_autograd_function_and_recompute(cuda):
     m2 = torch.as_tensor(m0, device=cuda).clone().requires_grad_(True)
     fwi.fwi_objective(m2, prob, Dobs).backward()
     torch.testing.assert_close(m2.grad, m.grad, rtol=1e-6, atol=1e-10 * m.grad.abs().max().item())
+
+
+def test_jacobian_adjoint_and_gauss_newton(cuda):
+    """testJacobian / testGaussNewton of test_ToolsAlgorithms3DFreqModeling.m:167-276:
+    Born data against a finite difference of the forward model, the dot test
+    <J dm, dD> = <dm, J' dD>, and HESS_GN(dm) = JACOB_ADJ(JACOB_FORW(dm))."""
+    import torch
+    from h3d import fwi
+
+    geom, m0, _ = _geometry("s2/m2", freqs=(5.0,))
+    prob = fwi.FWIProblem(geom, fwi.FWIConfig(tol=1e-11, precision="fp64"))
+    rng = np.random.default_rng(8)
+    dm = np.zeros(geom.n)
+    dm[1:-1, 1:-1, 1:-1] = rng.standard_normal((geom.n[0] - 2, geom.n[1] - 2, geom.n[2] - 2))
+    dm *= 1e-3 * np.abs(m0).max() / np.abs(dm).max()
+    mt, dmt = torch.as_tensor(m0, device=cuda), torch.as_tensor(dm, device=cuda)
+    Jdm = prob.jacob_forw(mt, dmt)
+    h = 0.1  # dm is already 1e-3 of m: central differences are accurate to ~1e-8 here
+    fd = (prob.forward_model(mt + h * dmt) - prob.forward_model(mt - h * dmt)) / (2 * h)
+    assert (fd - Jdm).abs().max().item() <= 1e-5 * Jdm.abs().max().item()
+    dD = torch.as_tensor(rng.standard_normal(Jdm.shape) + 1j * rng.standard_normal(Jdm.shape), device=cuda)
+    JtdD = prob.jacob_adj(mt, dD)
+    lhs = torch.sum(torch.conj(dD) * Jdm).real.item()
+    rhs = torch.sum(dmt * JtdD).item()
+    assert abs(lhs - rhs) <= 1e-8 * max(abs(lhs), abs(rhs))
+    hgn = prob.hess_gn(mt, dmt)
+    comp = prob.jacob_adj(mt, prob.jacob_forw(mt, dmt))
+    assert (hgn - comp).abs().max().item() <= 1e-9 * comp.abs().max().item()
