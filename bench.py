@@ -51,6 +51,28 @@ WORKLOAD = "config1: 201x201x101 incl. 20-pt PML, h=20 m, 6 Hz, single surface s
 REF_ITERS_CONFIG1 = 1481
 
 
+# Row order of the timed solves (the solver's tuner then picks the kernel configuration).
+DEFAULT_ORDER = "colour27"
+
+# DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of the
+# complex64 config-1 solve (python -m h3d.profile --kernel cgmn --config 1 --dtype c64,
+# the capture summarised in profiles/); keyed by (order, tuned variant).
+TRAFFIC_PER_LAUNCH = {}
+
+
+def _sweep_kernel(order, variant):
+    """Name, launches per double sweep and measured DRAM traffic per launch of the sweep
+    kernel the solver ran (variant: the tuner's choice reported in the solve info)."""
+    if order == "colour27":
+        name = ("sweep_direct_kernel<float> (COLOUR27 colour phase on stored coefficients)" if variant == 4
+                else f"sweep_tile_kernel<float> (COLOUR27 colour phase, tile shape {variant})")
+        return name, 54, TRAFFIC_PER_LAUNCH.get((order, variant))
+    if order == "block8":
+        return f"sweep_block8_kernel<float> (BLOCK8 parity phase, configuration {variant})", 16, \
+            TRAFFIC_PER_LAUNCH.get((order, variant))
+    return f"{order} sweep", None, None
+
+
 def _peaks():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
@@ -226,7 +248,7 @@ def run_gpu_arm(args, world, rank):
     N = m.N
     wn = torch.as_tensor(m.wavenumber(), device=dev)
     b = torch.as_tensor(m.point_source(), device=dev)
-    opts = solver.make_opts(tol=1e-6, precision="mixed", order="colour27", inner_tol=args.inner_tol,
+    opts = solver.make_opts(tol=1e-6, precision="mixed", order=args.order, inner_tol=args.inner_tol,
                             check_every=args.check_every)
 
     def step():
@@ -278,7 +300,7 @@ def run_gpu_arm(args, world, rank):
     fp64 = None
     if not args.skip_fp64:
         e0.record(st)
-        u64, info64 = solver.solve(grid, wn, b, tol=1e-6, precision="fp64", order="colour27",
+        u64, info64 = solver.solve(grid, wn, b, tol=1e-6, precision="fp64", order=args.order,
                                    check_every=args.check_every)
         e1.record(st)
         torch.cuda.synchronize()
@@ -287,17 +309,18 @@ def run_gpu_arm(args, world, rank):
         fp64 = {"solves_per_s": 1.0 / t64, "ms_per_solve": 1e3 * t64, "iters": info64["iters"],
                 "mixed_speedup": (1.0 / (elapsed / args.steps)) / (1.0 / t64),
                 "wavefield_rel_diff_mixed_vs_fp64": diff, "rel_res_true": info64["rel_res_true"]}
-    # roofline of the dominant kernel: the complex64 colour sweep, sampled live
+    # roofline of the dominant kernel: the complex64 sweep, sampled live
     sw_t = sum(i["sweep_seconds"] for i in infos)
     sw_n = sum(i["sweep_samples"] for i in infos)
     t_ds = sw_t / max(sw_n, 1)
-    launches_per_ds = 54
+    kernel, launches_per_ds, traffic = _sweep_kernel(args.order, infos[-1]["sweep_variant"])
+    launches_per_ds = launches_per_ds or 1  # other orders: figures per double sweep
     alg_bytes_ds = 2.0 * N * (2 * 8 + 4)
     peak, peak_kind = _peaks()
     achieved = alg_bytes_ds / t_ds / 1e9
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-            "traffic": args.traffic_per_launch, "kernel": "sweep_colour_kernel<float> (complex64 colour phase)",
-            "alg_bytes_per_launch": alg_bytes_ds / launches_per_ds,
+            "traffic": args.traffic_per_launch if args.traffic_per_launch is not None else traffic,
+            "kernel": kernel, "alg_bytes_per_launch": alg_bytes_ds / launches_per_ds,
             "avg_launch_us": 1e6 * t_ds / launches_per_ds, "samples": sw_n, "peak_source": peak_kind}
     cpu = None
     if not args.skip_cpu:
@@ -312,7 +335,8 @@ def run_gpu_arm(args, world, rank):
         "warmup": args.warmup, "ms_per_step": 1e3 * elapsed / args.steps, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c64 inner / f64 refinement",
         "data": "synthetic (seeded config-1 velocity model)",
-        "config": {"workload": WORKLOAD, "precision": "mixed", "order": "colour27",
+        "config": {"workload": WORKLOAD, "precision": "mixed", "order": args.order,
+                   "sweep_kernel": kernel,
                    "inner_tol": args.inner_tol, "l2": "working set > L2 (>= 340 MB per solve)",
                    "parallelism": f"replicas x{world}", "iters": infos[-1]["iters"],
                    "outer": infos[-1]["outer"], "rel_res_true": infos[-1]["rel_res_true"]},
@@ -329,6 +353,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="h3d", choices=["h3d", "reference"])
     ap.add_argument("--inner-tol", type=float, default=1e-4)
+    ap.add_argument("--order", default=DEFAULT_ORDER, choices=["colour27", "block8", "block", "lex"])
     ap.add_argument("--check-every", type=int, default=25)
     ap.add_argument("--cpu-sample-iters", type=int, default=4)
     ap.add_argument("--ref-iters", type=int, default=None)

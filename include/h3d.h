@@ -74,11 +74,19 @@ typedef enum { H3D_FORWARD = 1, H3D_ADJOINT = 2 } h3d_mode;
  *  COLOUR27  27 colour classes q = (i%3) + 3(j%3) + 9(k%3), ascending then descending.
  *  BLOCK     blocks of block[0..2] points visited by the block wavefront
  *            T = I + 2J + 4K, COLOUR27 order inside each block.
- * All three give a symmetric double sweep, hence a Hermitian positive
+ *  BLOCK8    blocks of block[0..2] points (12x12x12 or 24x12x12; 0 = tuned) in eight
+ *            parity classes p = I%2 + 2(J%2) + 4(K%2), ascending then descending,
+ *            COLOUR27 order inside each block; each block is processed in shared
+ *            memory, eight launches per pass.
+ * All four give a symmetric double sweep, hence a Hermitian positive
  * semi-definite I - Q for CGMN; they differ in the iterates, not the solution. */
-typedef enum { H3D_ORDER_LEX = 0, H3D_ORDER_COLOUR27 = 1, H3D_ORDER_BLOCK = 2 } h3d_order;
+typedef enum { H3D_ORDER_LEX = 0, H3D_ORDER_COLOUR27 = 1, H3D_ORDER_BLOCK = 2, H3D_ORDER_BLOCK8 = 3 } h3d_order;
 
 typedef enum { H3D_PREC_FP64 = 0, H3D_PREC_MIXED = 1 } h3d_precision;
+
+/* Krylov method on (I - Q) u = DSWP(0, b): CGMN (CGMN.m, the default of LinSolveOpts) or
+ * CRMN (CRMN.m, LinSolveOpts.SOLVE_CRMN); both dispatched by linearsolve.m:51-64. */
+typedef enum { H3D_METHOD_CGMN = 0, H3D_METHOD_CRMN = 1 } h3d_method;
 
 /* Stopping rules.  PRECONDITIONED is CGMN.m:79 (max over columns of the
  * preconditioned residual ratio <= tol); TRUE_RESIDUAL requires
@@ -101,9 +109,10 @@ typedef struct h3d_solve_opts {
     int32_t check_every;    /* iterations between host-visible convergence checks (graph length) */
     double inner_tol;       /* MIXED: relative tolerance of each complex64 inner solve */
     int32_t max_outer;      /* MIXED: maximum refinement steps */
-    int32_t block[3];       /* BLOCK order: block size (0 = choose automatically) */
+    int32_t block[3];       /* BLOCK / BLOCK8 orders: block size (0 = choose automatically) */
     int32_t use_graphs;     /* capture the iteration in a CUDA graph (1) or launch eagerly (0) */
     int32_t verbose;        /* print progress to stderr */
+    int32_t method;         /* h3d_method, default CGMN */
 } h3d_solve_opts;
 
 typedef struct h3d_solve_info {
@@ -116,7 +125,8 @@ typedef struct h3d_solve_info {
     double seconds;         /* wall time of the call (host clock, after stream sync) */
     double sweep_seconds;   /* sum of the sampled double-sweep device times (CUDA events) */
     int32_t sweep_samples;  /* number of double sweeps timed (one per replayed iteration block) */
-    int32_t pad_;
+    int32_t sweep_variant;  /* kernel configuration the tuner chose: COLOUR27 tile shape 0-3 or
+                               4 = stored row coefficients; BLOCK / BLOCK8 configuration */
     int64_t kernel_launches;/* device kernels this call executed (graph replays included) */
 } h3d_solve_info;
 
@@ -145,7 +155,10 @@ int h3d_mvp(const h3d_grid *g, const void *wn_re, const void *wn_im, const void 
             int nrhs, int mode, int deriv, int dtype, void *stream);
 
 /* One forward + backward Kaczmarz sweep with relaxation w on x (in place), right-hand
- * side b (NULL = 0).  Same element types as h3d_mvp. */
+ * side b (NULL = 0).  Same element types as h3d_mvp.  block: BLOCK / BLOCK8 block size
+ * (NULL or 0 = default); for COLOUR27, block[0] == -1 selects the shared-memory tile
+ * kernel instead of the kernel on stored row coefficients (27 N complex values of
+ * temporary device memory; used whenever they fit). */
 int h3d_kacz_sweep(const h3d_grid *g, const void *wn_re, const void *wn_im, double w, void *x,
                    const void *b, int nrhs, int mode, int order, const int32_t *block, int dtype,
                    void *stream);

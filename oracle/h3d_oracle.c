@@ -409,11 +409,34 @@ static void sweep_one(const op_t *op, const double *wnr, const double *wni, doub
         for (int q = 26; q >= 0; --q) colour_pass(op, wnr, wni, w, xr, xi, br, bi, adj, q, lo, hi, par);
         return;
     }
+    const int bx = blk[0], by = blk[1], bz = blk[2];
+    const int NI = (nx + bx - 1) / bx, NJ = (ny + by - 1) / by, NK = (nz + bz - 1) / bz;
+    if (order == H3DO_ORDER_BLOCK8) {
+        /* Blocks coloured by parity p = I%2 + 2(J%2) + 4(K%2), p ascending; two blocks
+         * of one parity are a whole block apart in some axis (blk >= 2), so their rows
+         * share no column and the order among them is immaterial.  27 colours inside a
+         * block.  The second pass reverses both levels. */
+        for (int pass = 0; pass < 2; ++pass)
+            for (int pp = 0; pp < 8; ++pp) {
+                const int p = pass == 0 ? pp : 7 - pp;
+                for (int bk = p >> 2; bk < NK; bk += 2)
+                    for (int bj = (p >> 1) & 1; bj < NJ; bj += 2)
+                        for (int bi_ = p & 1; bi_ < NI; bi_ += 2) {
+                            const int lo[3] = {bi_ * bx, bj * by, bk * bz};
+                            const int hi[3] = {lo[0] + bx < nx ? lo[0] + bx : nx,
+                                               lo[1] + by < ny ? lo[1] + by : ny,
+                                               lo[2] + bz < nz ? lo[2] + bz : nz};
+                            for (int qq = 0; qq < 27; ++qq) {
+                                const int q = pass == 0 ? qq : 26 - qq;
+                                colour_pass(op, wnr, wni, w, xr, xi, br, bi, adj, q, lo, hi, 0);
+                            }
+                        }
+            }
+        return;
+    }
     /* Block wavefront: blocks (I,J,K) of size blk, visited by T = I + 2J + 4K.
      * Adjacent blocks always differ in T and blocks sharing a T are never
      * adjacent, so the order among same-T blocks is immaterial. */
-    const int bx = blk[0], by = blk[1], bz = blk[2];
-    const int NI = (nx + bx - 1) / bx, NJ = (ny + by - 1) / by, NK = (nz + bz - 1) / bz;
     const int Tmax = (NI - 1) + 2 * (NJ - 1) + 4 * (NK - 1);
     for (int pass = 0; pass < 2; ++pass) {
         for (int tt = 0; tt <= Tmax; ++tt) {
@@ -441,7 +464,7 @@ int h3do_sweep(const h3do_grid *g, const double *wnr, const double *wni, double 
                const int *blk, int nthreads)
 {
     if (!g || nrhs < 1) return 1;
-    if (order == H3DO_ORDER_BLOCK && (!blk || blk[0] < 2 || blk[1] < 2 || blk[2] < 2)) return 2;
+    if ((order == H3DO_ORDER_BLOCK || order == H3DO_ORDER_BLOCK8) && (!blk || blk[0] < 2 || blk[1] < 2 || blk[2] < 2)) return 2;
     op_t op;
     op_make(&op, g);
     const size_t N = op.N;

@@ -28,7 +28,8 @@ typedef struct {
 enum {
     H3DO_ORDER_LEX = 0,      /* reference order: k, j, i ascending then descending */
     H3DO_ORDER_COLOUR27 = 1, /* 27 colours q = i%3 + 3(j%3) + 9(k%3), q ascending then descending */
-    H3DO_ORDER_BLOCK = 2     /* block-lexicographic wavefront, 27 colours inside each block */
+    H3DO_ORDER_BLOCK = 2,    /* block-lexicographic wavefront, 27 colours inside each block */
+    H3DO_ORDER_BLOCK8 = 3    /* blocks in 8 parity classes, 27 colours inside each block */
 };
 
 /* PML functions xi_lo / xi_hi of one axis at 0-based index idx in [-1, n]. */
@@ -46,7 +47,7 @@ int h3do_mvp(const h3do_grid *g, const double *wnr, const double *wni, const dou
              int nthreads);
 
 /* One forward + backward Kaczmarz sweep, in place on (xr, xi), nrhs columns.
- * br/bi may be NULL (b = 0).  blk = block dims for H3DO_ORDER_BLOCK. */
+ * br/bi may be NULL (b = 0).  blk = block dims for H3DO_ORDER_BLOCK and H3DO_ORDER_BLOCK8. */
 int h3do_sweep(const h3do_grid *g, const double *wnr, const double *wni, double w, double *xr,
                double *xi, const double *br, const double *bi, int nrhs, int adj, int order,
                const int *blk, int nthreads);

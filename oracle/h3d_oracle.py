@@ -16,7 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "_build", "libh3d_oracle.so")
 
-ORDER_LEX, ORDER_COLOUR27, ORDER_BLOCK = 0, 1, 2
+ORDER_LEX, ORDER_COLOUR27, ORDER_BLOCK, ORDER_BLOCK8 = 0, 1, 2, 3
 
 _lock = threading.Lock()
 _lib = None

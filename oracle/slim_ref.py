@@ -66,6 +66,50 @@ def cgmn(A, b, x, tol=1e-6, maxit=None, out_freq=0):
     return (x[:, 0] if squeeze else x), np.array(hst)
 
 
+# ---- CRMN.m:38-107 --------------------------------------------------------------------------
+def crmn(A, b, x=None, tol=1e-6, maxit=None):
+    """Conjugate residual with per-column gamma/beta; stops when max_j ||r_j||/||b_j|| <= tol
+    (CRMN.m:90).  ``A`` maps (N, P) arrays to (N, P) arrays; x None means a zero start
+    (CRMN.m:47-49: r = b without a product; linearsolve passes zeros, CRMN.m:51)."""
+    b = np.asarray(b, dtype=np.complex128)
+    squeeze = b.ndim == 1
+    if squeeze:
+        b = b[:, None]
+    if maxit is None:
+        maxit = b.shape[0]
+    if x is None:
+        r = b.copy()                                               # :48
+        x = np.zeros_like(b)
+    else:
+        x = np.asarray(x, dtype=np.complex128).reshape(b.shape)
+        r = b - A(x)                                               # :51
+    Ar = A(r)                                                      # :54
+    p, Ap = r.copy(), Ar.copy()                                    # :55-56
+    norm = lambda y: np.sqrt(np.sum(np.abs(y) ** 2, axis=0))       # :61-63
+    inner = lambda u, v: np.sum(np.conj(u) * v, axis=0)            # :60-64
+    nb, nr, nAp = norm(b), norm(r), norm(Ap)                       # :66-68
+    rAr = inner(r, Ar)                                             # :69
+    hst = [float(np.max(nr / nb))]                                 # :70
+    k = 0
+    while True:
+        gamma = rAr / nAp ** 2                                     # :73-77
+        x = x + p * gamma                                          # :79
+        r = r - Ap * gamma                                         # :80
+        nr = norm(r)                                               # :81
+        hst.append(float(np.max(nr / nb)))                         # :82-84
+        k += 1
+        if k >= maxit or hst[-1] <= tol:                           # :90-92
+            break
+        Ar = A(r)                                                  # :94
+        old = rAr
+        rAr = inner(r, Ar)                                         # :97
+        beta = rAr / old                                           # :98-102
+        p = r + p * beta                                           # :103
+        Ap = Ar + Ap * beta                                        # :104
+        nAp = norm(Ap)                                             # :105
+    return (x[:, 0] if squeeze else x), np.array(hst)
+
+
 # ---- linearsolve.m:148-156 with PREC_KACZSWP, solver CGMN -------------------------------------
 def linearsolve_cgmn(g, wn, b, mode=1, tol=1e-6, maxit=10000, order=O.ORDER_LEX, blk=None,
                      w=1.5, nthreads=None):
@@ -80,6 +124,19 @@ def linearsolve_cgmn(g, wn, b, mode=1, tol=1e-6, maxit=10000, order=O.ORDER_LEX,
 
     x0 = np.zeros_like(b)                                          # :117-119
     return cgmn(A, bt, x0, tol=tol, maxit=maxit)
+
+
+def linearsolve_crmn(g, wn, b, mode=1, tol=1e-6, maxit=10000, order=O.ORDER_LEX, blk=None,
+                     w=1.5, nthreads=None):
+    """linearsolve.m:148-156 with SOLVE_CRMN: CRMN on (I - Q) u = DSWP(0, b), zero start."""
+    adj = mode != 1
+    b = np.asarray(b, dtype=np.complex128)
+    bt = O.sweep(g, wn, w, np.zeros_like(b), b, adj=adj, order=order, blk=blk, nthreads=nthreads)
+
+    def A(y):
+        return y - O.sweep(g, wn, w, y, None, adj=adj, order=order, blk=blk, nthreads=nthreads)
+
+    return crmn(A, bt, np.zeros_like(b), tol=tol, maxit=maxit)
 
 
 def divide(g, wn, b, mode=1, **kw):

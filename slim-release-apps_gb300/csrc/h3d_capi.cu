@@ -11,7 +11,29 @@ using namespace h3d;
 
 namespace h3d {
 const char *last_error();
+
+// COLOUR27 runs on stored row coefficients (formed here for this call) unless block[0] is
+// -1 or they do not fit in device memory; then the shared-memory tile kernel runs.  Both
+// give the COLOUR27 result to rounding.
+template <typename T>
+static int kacz_sweep_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, bool adj, int order,
+                        const int32_t *block, cudaStream_t st)
+{
+    if (order == H3D_ORDER_COLOUR27 && !(block && block[0] == -1)) {
+        DevBuf cb, rb;
+        if (cb.alloc(sizeof(cplx<T>) * 27 * (size_t)op.N, st) == H3D_OK &&
+            rb.alloc(sizeof(T) * (size_t)op.N, st) == H3D_OK) {
+            int rc = store_row_coefs<T>(op, adj, cb.as<cplx<T>>(), st);
+            if (!rc) rc = row_inv_norms<T>(op, adj, rb.as<T>(), st);
+            if (!rc) rc = launch_sweep<T>(op, x, b, nrhs, w, adj, order, block, nullptr, st, rb.as<T>(), -1, cb.as<cplx<T>>());
+            return rc;
+        }
+        (void)cudaGetLastError();  // out of memory is not sticky: fall back to the tile kernel
+    }
+    return launch_sweep<T>(op, x, b, nrhs, w, adj, order, block, nullptr, st);
 }
+
+}  // namespace h3d
 
 extern "C" {
 
@@ -92,15 +114,15 @@ int h3d_kacz_sweep(const h3d_grid *g, const void *wn_re, const void *wn_im, doub
         Op<double> op;
         int rc = make_op_f64(g, (const double *)wn_re, (const double *)wn_im, &op);
         if (rc) return rc;
-        return launch_sweep<double>(op, (cplx<double> *)x, (const cplx<double> *)b, nrhs, w,
-                                    mode == H3D_ADJOINT, order, block, nullptr, st);
+        return kacz_sweep_t<double>(op, (cplx<double> *)x, (const cplx<double> *)b, nrhs, w,
+                                    mode == H3D_ADJOINT, order, block, st);
     }
     if (dtype == H3D_C64) {
         Op<float> op;
         int rc = make_op_f32(g, (const float *)wn_re, (const float *)wn_im, &op);
         if (rc) return rc;
-        return launch_sweep<float>(op, (cplx<float> *)x, (const cplx<float> *)b, nrhs, (float)w,
-                                   mode == H3D_ADJOINT, order, block, nullptr, st);
+        return kacz_sweep_t<float>(op, (cplx<float> *)x, (const cplx<float> *)b, nrhs, (float)w,
+                                   mode == H3D_ADJOINT, order, block, st);
     }
     set_error("h3d_kacz_sweep: unknown dtype %d", dtype);
     return H3D_ERR_BAD_ARG;

@@ -31,11 +31,19 @@ template <typename T>
 int launch_mvp(const Op<T> &op, const cplx<T> *x, cplx<T> *y, int nrhs, bool adj, bool deriv,
                cudaStream_t st);
 // rinv: optional 1/||a_i||^2 per row (COLOUR27 only; NULL = computed in the kernel);
-// shape: COLOUR27 tile shape index (-1 = chosen from the grid).
+// shape: COLOUR27 tile shape index (-1 = chosen from the grid).  coef (with rinv): stored
+// row coefficients; COLOUR27 then runs the direct kernel instead of the tile kernel.
 template <typename T>
 int launch_sweep(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, bool adj,
                  int order, const int32_t *block, const int *active, cudaStream_t st,
-                 const T *rinv = nullptr, int shape = -1);
+                 const T *rinv = nullptr, int shape = -1, const cplx<T> *coef = nullptr);
+
+// h3d_sweep_direct.cu: COLOUR27 on stored row coefficients (27 N complex values, colour-major).
+template <typename T>
+int store_row_coefs(const Op<T> &op, bool adj, cplx<T> *coef, cudaStream_t st);
+template <typename T>
+int sweep_colour_direct(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active,
+                        const T *rinv, const cplx<T> *coef, bool adj, cudaStream_t st);
 
 // h3d_sweep_tile.cu: one COLOUR27 pass (27 colour launches) with shared-memory boxes.
 template <typename T>
@@ -48,8 +56,24 @@ int pick_tile_shape(int nx, int ny, int nz);
 int num_tile_shapes();
 
 // h3d_block.cu: the BLOCK ordering (block wavefront, 27 colours inside a block).
+// cfg: index of a compiled (block shape, right-hand-side group) configuration, or -1 to
+// derive it from `block` (8x8x8 by default).
 template <typename T>
 int sweep_block(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w,
-                const int32_t *block, const int *active, bool adj, cudaStream_t st);
+                const int32_t *block, const int *active, bool adj, cudaStream_t st,
+                const T *rinv = nullptr, int cfg = -1);
+int num_block_cfgs();
+void block_cfg_dims(int c, int32_t *blk, int *r);
+size_t block_cfg_smem(int c, bool fp64, bool wnc);
+
+// h3d_block8.cu: the BLOCK8 ordering (eight parity classes of blocks, 27 colours inside a
+// block); cfg as for sweep_block (12x12x12 by default).
+template <typename T>
+int sweep_block8(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w,
+                 const int32_t *block, const int *active, bool adj, cudaStream_t st,
+                 const T *rinv = nullptr, int cfg = -1);
+int num_block8_cfgs();
+void block8_cfg_dims(int c, int32_t *blk, int *r);
+size_t block8_cfg_smem(int c, bool fp64, bool wnc);
 
 }  // namespace h3d

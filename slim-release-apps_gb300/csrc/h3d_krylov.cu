@@ -14,8 +14,8 @@ namespace h3d {
 
 int reduction_blocks(long long N)
 {
-    long long g = (N + 4LL * kVecThreads - 1) / (4LL * kVecThreads);
-    if (g > 304) g = 304;
+    long long g = (N + (long long)kVecUnroll * kVecThreads - 1) / ((long long)kVecUnroll * kVecThreads);
+    if (g > 608) g = 608;  // four 256-thread blocks per SM
     if (g < 1) g = 1;
     return (int)g;
 }
@@ -125,16 +125,28 @@ __global__ void k_ap_dot(const cplx<T> *__restrict__ p, cplx<T> *__restrict__ y,
 {
     const int s = blockIdx.y;
     if (!active[s]) return;
-    const long long off = (long long)s * N;
+    const cplx<T> *ps = p + (long long)s * N;
+    cplx<T> *ys = y + (long long)s * N;
     double are = 0.0, aim = 0.0;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < N;
-         q += (long long)G * blockDim.x) {
-        const cplx<T> pv = p[off + q], yv = y[off + q];
+    auto body = [&](const cplx<T> pv, const cplx<T> yv, long long q) {
         const cplx<T> ap = pv - yv;
-        y[off + q] = ap;
+        ys[q] = ap;
         are += (double)pv.re * ap.re + (double)pv.im * ap.im;
         aim += (double)pv.re * ap.im - (double)pv.im * ap.re;
+    };
+    const long long stride = (long long)G * blockDim.x;
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; q + (kVecUnroll - 1) * stride < N; q += kVecUnroll * stride) {
+        cplx<T> pv[kVecUnroll], yv[kVecUnroll];
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            pv[u] = ps[q + u * stride];
+            yv[u] = ys[q + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) body(pv[u], yv[u], q + u * stride);
     }
+    for (; q < N; q += stride) body(ps[q], ys[q], q);
     const double2 t = block_sum2(are, aim);
     if (threadIdx.x == 0) {
         part[2 * ((long long)s * G + blockIdx.x)] = t.x;
@@ -181,18 +193,32 @@ __global__ void k_update_xr(cplx<T> *__restrict__ x, cplx<T> *__restrict__ r,
     const int s = blockIdx.y;
     if (!active[s]) return;
     const long long off = (long long)s * N;
+    cplx<T> *xs = x + off, *rs = r + off;
+    const cplx<T> *ps = p + off, *as = ap + off;
     const cplx<T> a = mk<T>((T)alpha[2 * s], (T)alpha[2 * s + 1]);
     double acc = 0.0;
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < N;
-         q += (long long)G * blockDim.x) {
-        const cplx<T> pv = p[off + q], av = ap[off + q];
-        cplx<T> xv = x[off + q], rv = r[off + q];
+    auto body = [&](const cplx<T> pv, const cplx<T> av, cplx<T> xv, cplx<T> rv, long long q) {
         xv = xv + pv * a;
         rv = rv - av * a;
-        x[off + q] = xv;
-        r[off + q] = rv;
+        xs[q] = xv;
+        rs[q] = rv;
         acc += (double)rv.re * rv.re + (double)rv.im * rv.im;
+    };
+    const long long stride = (long long)G * blockDim.x;
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; q + (kVecUnroll - 1) * stride < N; q += kVecUnroll * stride) {
+        cplx<T> pv[kVecUnroll], av[kVecUnroll], xv[kVecUnroll], rv[kVecUnroll];
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            pv[u] = ps[q + u * stride];
+            av[u] = as[q + u * stride];
+            xv[u] = xs[q + u * stride];
+            rv[u] = rs[q + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) body(pv[u], av[u], xv[u], rv[u], q + u * stride);
     }
+    for (; q < N; q += stride) body(ps[q], as[q], xs[q], rs[q], q);
     const double2 t = block_sum2(acc, 0.0);
     if (threadIdx.x == 0) {
         part[2 * ((long long)s * G + blockIdx.x)] = t.x;
@@ -246,12 +272,29 @@ __global__ void k_update_p(cplx<T> *__restrict__ p, const cplx<T> *__restrict__ 
     const int s = blockIdx.y;
     if (!upd[s]) return;
     const long long off = (long long)s * N;
+    cplx<T> *ps = p + off, *ys = y + off;
+    const cplx<T> *rs = r + off;
     const T b = (T)beta[s];
-    for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < N;
-         q += (long long)G * blockDim.x) {
-        const cplx<T> v = r[off + q] + b * p[off + q];
-        p[off + q] = v;
-        y[off + q] = v;
+    const long long stride = (long long)G * blockDim.x;
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; q + (kVecUnroll - 1) * stride < N; q += kVecUnroll * stride) {
+        cplx<T> rv[kVecUnroll], pv[kVecUnroll];
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            rv[u] = rs[q + u * stride];
+            pv[u] = ps[q + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            const cplx<T> v = rv[u] + b * pv[u];
+            ps[q + u * stride] = v;
+            ys[q + u * stride] = v;
+        }
+    }
+    for (; q < N; q += stride) {
+        const cplx<T> v = rs[q] + b * ps[q];
+        ps[q] = v;
+        ys[q] = v;
     }
 }
 
@@ -260,6 +303,169 @@ int cg_update_p(cplx<T> *p, const cplx<T> *r, cplx<T> *y, long long N, int nrhs,
                 const CgState &s, cudaStream_t st)
 {
     k_update_p<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(p, r, y, N, s.upd, s.beta, s.G);
+    H3D_CUDA_TRY(cudaGetLastError());
+    return H3D_OK;
+}
+
+// ---- CRMN ------------------------------------------------------------------------------
+// x += gamma p; r -= gamma Ap; y = r; partial ||r||^2 (CRMN.m:79-81).
+template <typename T>
+__global__ void k_cr_update_xr(cplx<T> *__restrict__ x, cplx<T> *__restrict__ r,
+                               const cplx<T> *__restrict__ p, const cplx<T> *__restrict__ ap,
+                               cplx<T> *__restrict__ y, long long N, const int *__restrict__ active,
+                               const double *__restrict__ gamma, double *part, int G)
+{
+    const int s = blockIdx.y;
+    if (!active[s]) return;
+    const long long off = (long long)s * N;
+    cplx<T> *xs = x + off, *rs = r + off, *ys = y + off;
+    const cplx<T> *ps = p + off, *as = ap + off;
+    const cplx<T> g = mk<T>((T)gamma[2 * s], (T)gamma[2 * s + 1]);
+    double acc = 0.0;
+    auto body = [&](const cplx<T> pv, const cplx<T> av, cplx<T> xv, cplx<T> rv, long long q) {
+        xv = xv + pv * g;
+        rv = rv - av * g;
+        xs[q] = xv;
+        rs[q] = rv;
+        ys[q] = rv;
+        acc += (double)rv.re * rv.re + (double)rv.im * rv.im;
+    };
+    const long long stride = (long long)G * blockDim.x;
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; q + (kVecUnroll - 1) * stride < N; q += kVecUnroll * stride) {
+        cplx<T> pv[kVecUnroll], av[kVecUnroll], xv[kVecUnroll], rv[kVecUnroll];
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            pv[u] = ps[q + u * stride];
+            av[u] = as[q + u * stride];
+            xv[u] = xs[q + u * stride];
+            rv[u] = rs[q + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) body(pv[u], av[u], xv[u], rv[u], q + u * stride);
+    }
+    for (; q < N; q += stride) body(ps[q], as[q], xs[q], rs[q], q);
+    const double2 t = block_sum2(acc, 0.0);
+    if (threadIdx.x == 0) {
+        part[2 * ((long long)s * G + blockIdx.x)] = t.x;
+        part[2 * ((long long)s * G + blockIdx.x) + 1] = 0.0;
+    }
+}
+
+template <typename T>
+int cr_update_xr(cplx<T> *x, cplx<T> *r, const cplx<T> *p, const cplx<T> *ap, cplx<T> *y,
+                 long long N, int nrhs, const CgState &s, int maxit, cudaStream_t st)
+{
+    k_cr_update_xr<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(x, r, p, ap, y, N, s.active, s.alpha,
+                                                               s.part, s.G);
+    k_beta<<<nrhs, kVecThreads, 0, st>>>(s, maxit);  // ||r||, iteration count, stop test
+    H3D_CUDA_TRY(cudaGetLastError());
+    return H3D_OK;
+}
+
+// Ar = r - y over y and partial <r, Ar> (CRMN.m:94-97): the CGMN kernel with p -> r.
+template <typename T>
+int cr_ar_dot(const cplx<T> *r, cplx<T> *y, long long N, int nrhs, const CgState &s, cudaStream_t st)
+{
+    k_ap_dot<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(r, y, N, s.active, s.part, s.G);
+    H3D_CUDA_TRY(cudaGetLastError());
+    return H3D_OK;
+}
+
+// beta = rAr_new / rAr_old (complex; 0 on the first call); rAr_old = rAr_new (CRMN.m:96-102).
+__global__ void k_cr_beta(CgState st, int first)
+{
+    const int s = blockIdx.x;
+    if (!st.active[s]) return;
+    const double2 rar = sum_partials(st.part, st.G, s);
+    if (threadIdx.x == 0) {
+        double br = 0.0, bi = 0.0;
+        if (!first) {
+            const double orr = st.rar[2 * s], oi = st.rar[2 * s + 1];
+            const double d = orr * orr + oi * oi;
+            br = (rar.x * orr + rar.y * oi) / d;
+            bi = (rar.y * orr - rar.x * oi) / d;
+            if (!(d > 0.0) || !isfinite(br) || !isfinite(bi)) {
+                br = bi = 0.0;
+                st.status[s] = H3D_ERR_NONFINITE;
+            }
+        }
+        st.cbeta[2 * s] = br;
+        st.cbeta[2 * s + 1] = bi;
+        st.rar[2 * s] = rar.x;
+        st.rar[2 * s + 1] = rar.y;
+    }
+}
+
+// p = r + beta p; Ap = Ar + beta Ap; partial ||Ap||^2 (CRMN.m:103-105).
+template <typename T>
+__global__ void k_cr_update_p(cplx<T> *__restrict__ p, cplx<T> *__restrict__ ap,
+                              const cplx<T> *__restrict__ r, const cplx<T> *__restrict__ ar, long long N,
+                              const int *__restrict__ active, const double *__restrict__ cbeta,
+                              double *part, int G)
+{
+    const int s = blockIdx.y;
+    if (!active[s]) return;
+    const long long off = (long long)s * N;
+    cplx<T> *ps = p + off, *aps = ap + off;
+    const cplx<T> *rs = r + off, *ars = ar + off;
+    const cplx<T> b = mk<T>((T)cbeta[2 * s], (T)cbeta[2 * s + 1]);
+    double acc = 0.0;
+    auto body = [&](const cplx<T> rv, const cplx<T> arv, const cplx<T> pv, const cplx<T> apv, long long q) {
+        const cplx<T> pn = rv + pv * b;
+        const cplx<T> an = arv + apv * b;
+        ps[q] = pn;
+        aps[q] = an;
+        acc += (double)an.re * an.re + (double)an.im * an.im;
+    };
+    const long long stride = (long long)G * blockDim.x;
+    long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    for (; q + (kVecUnroll - 1) * stride < N; q += kVecUnroll * stride) {
+        cplx<T> rv[kVecUnroll], arv[kVecUnroll], pv[kVecUnroll], apv[kVecUnroll];
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) {
+            rv[u] = rs[q + u * stride];
+            arv[u] = ars[q + u * stride];
+            pv[u] = ps[q + u * stride];
+            apv[u] = aps[q + u * stride];
+        }
+#pragma unroll
+        for (int u = 0; u < kVecUnroll; ++u) body(rv[u], arv[u], pv[u], apv[u], q + u * stride);
+    }
+    for (; q < N; q += stride) body(rs[q], ars[q], ps[q], aps[q], q);
+    const double2 t = block_sum2(acc, 0.0);
+    if (threadIdx.x == 0) {
+        part[2 * ((long long)s * G + blockIdx.x)] = t.x;
+        part[2 * ((long long)s * G + blockIdx.x) + 1] = 0.0;
+    }
+}
+
+// gamma = rAr / ||Ap||^2 (complex over real, CRMN.m:73-77).
+__global__ void k_cr_gamma(CgState st)
+{
+    const int s = blockIdx.x;
+    if (!st.active[s]) return;
+    const double2 n = sum_partials(st.part, st.G, s);
+    if (threadIdx.x == 0) {
+        st.nap2[s] = n.x;
+        double gr = st.rar[2 * s] / n.x, gi = st.rar[2 * s + 1] / n.x;
+        if (!(n.x > 0.0) || !isfinite(gr) || !isfinite(gi)) {
+            gr = gi = 0.0;
+            st.status[s] = H3D_ERR_NONFINITE;
+        }
+        st.alpha[2 * s] = gr;
+        st.alpha[2 * s + 1] = gi;
+    }
+}
+
+template <typename T>
+int cr_update_p(cplx<T> *p, cplx<T> *ap, const cplx<T> *r, const cplx<T> *ar, long long N, int nrhs,
+                const CgState &s, bool first, cudaStream_t st)
+{
+    k_cr_beta<<<nrhs, kVecThreads, 0, st>>>(s, first ? 1 : 0);
+    k_cr_update_p<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(p, ap, r, ar, N, s.active, s.cbeta,
+                                                              s.part, s.G);
+    k_cr_gamma<<<nrhs, kVecThreads, 0, st>>>(s);
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;
 }
@@ -353,6 +559,11 @@ int add_scaled_c64(cplx<double> *u, const cplx<float> *e, long long N, int nrhs,
                                  int, const CgState &, int, cudaStream_t);                             \
     template int cg_update_p<T>(cplx<T> *, const cplx<T> *, cplx<T> *, long long, int,                 \
                                 const CgState &, cudaStream_t);                                        \
+    template int cr_update_xr<T>(cplx<T> *, cplx<T> *, const cplx<T> *, const cplx<T> *, cplx<T> *,    \
+                                 long long, int, const CgState &, int, cudaStream_t);                  \
+    template int cr_ar_dot<T>(const cplx<T> *, cplx<T> *, long long, int, const CgState &, cudaStream_t); \
+    template int cr_update_p<T>(cplx<T> *, cplx<T> *, const cplx<T> *, const cplx<T> *, long long, int, \
+                                const CgState &, bool, cudaStream_t);                                  \
     template int copy_active<T>(const cplx<T> *, cplx<T> *, long long, int, const int *, cudaStream_t); \
     template int zero_vec<T>(cplx<T> *, long long, int, cudaStream_t);
 H3D_INST(double)

@@ -23,9 +23,13 @@ struct CgState {
     int *status;      // 0 ok, H3D_ERR_NONFINITE on NaN/Inf
     double *part;     // reduction partials: nrhs x G x 2
     int G;            // reduction blocks per RHS
+    // CRMN only (null for CGMN): complex <r, A r> (re, im) pairs, complex beta pairs,
+    // ||A p||^2; alpha holds gamma.
+    double *rar = nullptr, *cbeta = nullptr, *nap2 = nullptr;
 };
 
 constexpr int kVecThreads = 256;
+constexpr int kVecUnroll = 4;  // independent elements per thread and loop step
 
 template <typename T>
 int cg_init(const cplx<T> *bt, cplx<T> *x, cplx<T> *r, cplx<T> *p, long long N, int nrhs,
@@ -40,6 +44,21 @@ int cg_update_xr(cplx<T> *x, cplx<T> *r, const cplx<T> *p, const cplx<T> *ap, lo
 template <typename T>
 int cg_update_p(cplx<T> *p, const cplx<T> *r, cplx<T> *y, long long N, int nrhs,
                 const CgState &s, cudaStream_t st);
+// CRMN building blocks (CRMN.m:54-105), on the same masks and reductions.
+//   cr_update_xr: x += gamma p; r -= gamma Ap; y = r (the next sweep's input); ||r||^2 and
+//                 the stop test (CRMN.m:79-92)
+//   cr_ar_dot:    Ar = r - y over y, <r, Ar>                        (CRMN.m:94-97)
+//   cr_update_p:  beta = rAr / rAr_old (0 when first); p = r + beta p; Ap = Ar + beta Ap;
+//                 ||Ap||^2; gamma = rAr / ||Ap||^2                   (CRMN.m:73-77, 98-105)
+template <typename T>
+int cr_update_xr(cplx<T> *x, cplx<T> *r, const cplx<T> *p, const cplx<T> *ap, cplx<T> *y,
+                 long long N, int nrhs, const CgState &s, int maxit, cudaStream_t st);
+template <typename T>
+int cr_ar_dot(const cplx<T> *r, cplx<T> *y, long long N, int nrhs, const CgState &s, cudaStream_t st);
+template <typename T>
+int cr_update_p(cplx<T> *p, cplx<T> *ap, const cplx<T> *r, const cplx<T> *ar, long long N,
+                int nrhs, const CgState &s, bool first, cudaStream_t st);
+
 template <typename T>
 int copy_active(const cplx<T> *src, cplx<T> *dst, long long N, int nrhs, const int *active,
                 cudaStream_t st);

@@ -86,11 +86,15 @@ struct CgRun {
     int order = H3D_ORDER_COLOUR27;
     int32_t block[3] = {0, 0, 0};
     int maxit = 10000;
+    int method = H3D_METHOD_CGMN;
+    int verbose = 0;
     cplx<T> *x = nullptr, *r = nullptr, *p = nullptr, *y = nullptr;
-    T *rinv = nullptr;   // 1/||a_i||^2 per row, computed once (COLOUR27)
-    int shape = -1;      // COLOUR27 tile shape
+    cplx<T> *ap = nullptr;  // CRMN: A p
+    T *rinv = nullptr;   // 1/||a_i||^2 per row, computed once (all orders but LEX)
+    int shape = -1;      // COLOUR27 tile shape (num_tile_shapes(): stored coefficients), BLOCK cfg
+    cplx<T> *coef = nullptr;  // COLOUR27 stored row coefficients (27 N), when they fit
     CgState s{};
-    DevBuf vecs, scal, ints, parts, norms;
+    DevBuf vecs, scal, ints, parts, norms, coefs;
     cudaGraphExec_t exec = nullptr;
     int graph_iters = 0;
     // Timing of the last double sweep of every replayed block: two timing events recorded
@@ -109,7 +113,7 @@ struct CgRun {
         if (ev1) cudaEventDestroy(ev1);
     }
 
-    int iteration_launches() const { return sweep_launches() + 5; }
+    int iteration_launches() const { return sweep_launches() + (method == H3D_METHOD_CRMN ? 6 : 5); }
 
     // Fold the last timed sweep into the totals (the stream has been synchronised).
     void harvest_timing()
@@ -127,13 +131,15 @@ struct CgRun {
     {
         const size_t vb = sizeof(cplx<T>) * (size_t)N * nrhs;
         int rc;
-        if ((rc = vecs.alloc(4 * vb, st))) return rc;
+        const bool cr = method == H3D_METHOD_CRMN;
+        if ((rc = vecs.alloc((cr ? 5 : 4) * vb, st))) return rc;
         x = vecs.as<cplx<T>>();
         r = x + N * nrhs;
         p = r + N * nrhs;
         y = p + N * nrhs;
+        ap = cr ? y + N * nrhs : nullptr;
         s.G = reduction_blocks(N);
-        if ((rc = scal.alloc(sizeof(double) * (size_t)nrhs * 7, st))) return rc;
+        if ((rc = scal.alloc(sizeof(double) * (size_t)nrhs * (cr ? 12 : 7), st))) return rc;
         double *d = scal.as<double>();
         s.rr = d;
         s.bb = d + nrhs;
@@ -141,6 +147,11 @@ struct CgRun {
         s.tolp = d + 3 * nrhs;
         s.beta = d + 4 * nrhs;
         s.alpha = d + 5 * nrhs;  // 2 * nrhs
+        if (cr) {
+            s.rar = d + 7 * nrhs;    // 2 * nrhs
+            s.cbeta = d + 9 * nrhs;  // 2 * nrhs
+            s.nap2 = d + 11 * nrhs;
+        }
         if ((rc = ints.alloc(sizeof(int) * (size_t)nrhs * 4, st))) return rc;
         int *q = ints.as<int>();
         s.active = q;
@@ -149,11 +160,22 @@ struct CgRun {
         s.status = q + 3 * nrhs;
         if ((rc = parts.alloc(sizeof(double) * 2 * (size_t)s.G * nrhs, st))) return rc;
         s.part = parts.as<double>();
-        if (order == H3D_ORDER_COLOUR27) {
+        if (order != H3D_ORDER_LEX) {
             if ((rc = norms.alloc(sizeof(T) * (size_t)N, st))) return rc;
             rinv = norms.as<T>();
             if ((rc = row_inv_norms<T>(op, adj, rinv, st))) return rc;
             ++launches;
+        }
+        if (order == H3D_ORDER_COLOUR27) {
+            // stored coefficients when they take at most half of the free device memory
+            size_t fr = 0, tot = 0;
+            const size_t bytes = sizeof(cplx<T>) * 27 * (size_t)N;
+            if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2 && coefs.alloc(bytes, st) == H3D_OK) {
+                coef = coefs.as<cplx<T>>();
+                if ((rc = store_row_coefs<T>(op, adj, coef, st))) return rc;
+                launches += 27;
+            }
+            (void)cudaGetLastError();
         }
         return H3D_OK;
     }
@@ -162,11 +184,16 @@ struct CgRun {
     {
         if (order == H3D_ORDER_LEX) return 2 * ((op.nx - 1) + 3 * (op.ny - 1) + 9 * (op.nz - 1) + 1);
         if (order == H3D_ORDER_BLOCK) {
-            const int bx = block[0] > 0 ? block[0] : 8, by = block[1] > 0 ? block[1] : 8,
-                      bz = block[2] > 0 ? block[2] : 8;
+            int32_t bd[3] = {block[0] > 0 ? block[0] : 8, block[1] > 0 ? block[1] : 8, block[2] > 0 ? block[2] : 8};
+            if (shape >= 0) {
+                int r = 1;
+                block_cfg_dims(shape, bd, &r);
+            }
+            const int bx = bd[0], by = bd[1], bz = bd[2];
             return 2 * (((op.nx + bx - 1) / bx - 1) + 2 * ((op.ny + by - 1) / by - 1) +
                         4 * ((op.nz + bz - 1) / bz - 1) + 1);
         }
+        if (order == H3D_ORDER_BLOCK8) return 16;
         int n = 0;
         for (int q = 0; q < 27; ++q) {
             const int a = q % 3, bq = (q / 3) % 3, cq = q / 9;
@@ -180,24 +207,49 @@ struct CgRun {
     // and keep the fastest; decisions are cached per (grid, precision, mode, nrhs).
     int tune(cudaStream_t st)
     {
-        if (order != H3D_ORDER_COLOUR27 || shape >= 0) return H3D_OK;
-        const TuneKey key{op.nx, op.ny, op.nz, (int)sizeof(T), adj ? 1 : 0, op.wni ? 1 : 0, nrhs};
-        if (tune_lookup(key, &shape)) return H3D_OK;
+        if (order == H3D_ORDER_LEX || shape >= 0) return H3D_OK;
+        if (order != H3D_ORDER_COLOUR27 && block[0] > 0) return H3D_OK;  // explicit block size
+        const TuneKey key{op.nx, op.ny, op.nz, (int)sizeof(T) + 100 * order, adj ? 1 : 0, op.wni ? 1 : 0, nrhs};
+        if (tune_lookup(key, &shape)) {
+            settle_coefs();
+            return H3D_OK;
+        }
         cudaEvent_t e0, e1;
         H3D_CUDA_TRY(cudaEventCreate(&e0));
         H3D_CUDA_TRY(cudaEventCreate(&e1));
         float best = 1e30f;
         int best_shape = 0;
         int rc = zero_vec<T>(y, N, nrhs, st);
-        for (int sh = 0; sh < num_tile_shapes() && !rc; ++sh) {
-            if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, nullptr, st, rinv, sh))) break;
+        const int ncand = order == H3D_ORDER_BLOCK    ? num_block_cfgs()
+                          : order == H3D_ORDER_BLOCK8 ? num_block8_cfgs()
+                                                      : num_tile_shapes() + (coef ? 1 : 0);
+        for (int sh = 0; sh < ncand && !rc; ++sh) {
+            if (order != H3D_ORDER_COLOUR27) {
+                int32_t bd[3];
+                int r = 1;
+                const bool f64 = sizeof(T) == 8, wnc = op.wni != nullptr;
+                size_t smem;
+                if (order == H3D_ORDER_BLOCK) {
+                    block_cfg_dims(sh, bd, &r);
+                    smem = block_cfg_smem(sh, f64, wnc);
+                } else {
+                    block8_cfg_dims(sh, bd, &r);
+                    smem = block8_cfg_smem(sh, f64, wnc);
+                }
+                // only groups the right-hand sides fill, and configurations that fit
+                if (r > nrhs || smem == 0) continue;
+            }
+            const cplx<T> *cf = (order == H3D_ORDER_COLOUR27 && sh == num_tile_shapes()) ? coef : nullptr;
+            if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, nullptr, st, rinv, sh, cf))) break;
             cudaEventRecord(e0, st);
             for (int rep = 0; rep < 2 && !rc; ++rep)
-                rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, nullptr, st, rinv, sh);
+                rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, nullptr, st, rinv, sh, cf);
             cudaEventRecord(e1, st);
             cudaEventSynchronize(e1);
             float ms = 0.f;
             cudaEventElapsedTime(&ms, e0, e1);
+            if (verbose)
+                fprintf(stderr, "[h3d] tune order %d candidate %d: %.3f ms per double sweep\n", order, sh, 0.5 * ms);
             if (ms < best) {
                 best = ms;
                 best_shape = sh;
@@ -209,8 +261,24 @@ struct CgRun {
         if (rc) return rc;
         shape = best_shape;
         tune_store(key, shape);
+        settle_coefs();
         return H3D_OK;
     }
+
+    // COLOUR27: keep the stored coefficients only if the chosen implementation uses them
+    // (a cached choice of them without room for them falls back to the grid's tile shape).
+    void settle_coefs()
+    {
+        if (order != H3D_ORDER_COLOUR27) return;
+        if (shape == num_tile_shapes() && !coef) shape = pick_tile_shape(op.nx, op.ny, op.nz);
+        if (shape != num_tile_shapes() && coef) {
+            coefs.release();
+            coef = nullptr;
+        }
+    }
+
+    // Stored coefficients for the sweep launches (null: the chosen kernel does not use them).
+    const cplx<T> *cf() const { return (order == H3D_ORDER_COLOUR27 && shape == num_tile_shapes()) ? coef : nullptr; }
 
     // b~ = DSWP(0, b) into y, then x = 0, r = p = y.
     int setup(const cplx<T> *b, const double *bnorm2_orig, double zero_tol2, cudaStream_t st)
@@ -218,16 +286,38 @@ struct CgRun {
         int rc;
         if ((rc = tune(st))) return rc;
         if ((rc = zero_vec<T>(y, N, nrhs, st))) return rc;
-        if ((rc = launch_sweep<T>(op, y, b, nrhs, w, adj, order, block, nullptr, st, rinv, shape))) return rc;
+        if ((rc = launch_sweep<T>(op, y, b, nrhs, w, adj, order, block, nullptr, st, rinv, shape, cf()))) return rc;
         launches += sweep_launches() + 2;
-        return cg_init<T>(y, x, r, p, N, nrhs, s, bnorm2_orig, zero_tol2, maxit, st);
+        if ((rc = cg_init<T>(y, x, r, p, N, nrhs, s, bnorm2_orig, zero_tol2, maxit, st))) return rc;
+        if (method != H3D_METHOD_CRMN) return H3D_OK;
+        // CRMN.m:54-56, 66-69 with the zero start of linearsolve: r = b~ (y holds it too),
+        // Ar = A r, p = r, Ap = Ar, gamma; then the first x, r update and stop test
+        // (CRMN.m:79-92).  Every later iteration starts at Ar = A r (CRMN.m:94), so a
+        // right-hand side stopped by the test resumes exactly where CRMN.m would continue.
+        if ((rc = zero_vec<T>(ap, N, nrhs, st))) return rc;
+        if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st, rinv, shape, cf()))) return rc;
+        if ((rc = cr_ar_dot<T>(r, y, N, nrhs, s, st))) return rc;
+        if ((rc = cr_update_p<T>(p, ap, r, y, N, nrhs, s, true, st))) return rc;
+        if ((rc = cr_update_xr<T>(x, r, p, ap, y, N, nrhs, s, maxit, st))) return rc;
+        launches += sweep_launches() + 6;
+        return H3D_OK;
     }
 
     int enqueue_iteration(cudaStream_t st, bool timed)
     {
         int rc;
+        if (method == H3D_METHOD_CRMN) {
+            // CRMN.m:94-105 then 73-92: Ar = A r (y = r on entry), rAr, beta, p, Ap, ||Ap||,
+            // gamma; x, r, y = r, the stop test
+            if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev0, st, cudaEventRecordExternal));
+            if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st, rinv, shape, cf()))) return rc;
+            if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev1, st, cudaEventRecordExternal));
+            if ((rc = cr_ar_dot<T>(r, y, N, nrhs, s, st))) return rc;
+            if ((rc = cr_update_p<T>(p, ap, r, y, N, nrhs, s, false, st))) return rc;
+            return cr_update_xr<T>(x, r, p, ap, y, N, nrhs, s, maxit, st);
+        }
         if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev0, st, cudaEventRecordExternal));
-        if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st, rinv, shape))) return rc;
+        if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st, rinv, shape, cf()))) return rc;
         if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev1, st, cudaEventRecordExternal));
         if ((rc = cg_ap_dot<T>(p, y, N, nrhs, s, st))) return rc;
         if ((rc = cg_update_xr<T>(x, r, p, y, N, nrhs, s, maxit, st))) return rc;
@@ -379,7 +469,7 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
     if ((rc = residual_f64(op64, b, u, r64, rr2, bb2, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
     long long extra_launches = 2;
     double sw_sec = 0.0;
-    int sw_n = 0;
+    int sw_n = 0, sw_variant = -1;
     long long cg_launches = 0;
 
     std::vector<double> h_rr(nrhs), h_bb(nrhs);
@@ -414,6 +504,8 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         cg.order = o.order;
         std::memcpy(cg.block, o.block, sizeof cg.block);
         cg.maxit = o.maxit;
+        cg.method = o.method;
+        cg.verbose = o.verbose;
         if ((rc = cg.alloc(st))) return rc;
         std::vector<double> tolp(nrhs, o.tol);
         H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, st));
@@ -452,6 +544,7 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         }
         sw_sec = cg.sweep_seconds;
         sw_n = cg.sweep_samples;
+        sw_variant = cg.shape;
         cg_launches = cg.launches;
     } else {
         // Mixed precision: complex64 CGMN on the scaled FP64 residual, FP64 update and residual.
@@ -474,6 +567,8 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         cg.order = o.order;
         std::memcpy(cg.block, o.block, sizeof cg.block);
         cg.maxit = o.maxit;
+        cg.method = o.method;
+        cg.verbose = o.verbose;
         if ((rc = cg.alloc(st))) return rc;
         DevBuf actb;
         if ((rc = actb.alloc(sizeof(int) * nrhs, st))) return rc;
@@ -508,6 +603,7 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         }
         sw_sec = cg.sweep_seconds;
         sw_n = cg.sweep_samples;
+        sw_variant = cg.shape;
         cg_launches = cg.launches;
     }
     bool all_ok = !nonfinite;
@@ -533,7 +629,7 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         info->seconds = timer.seconds();
         info->sweep_seconds = sw_sec;
         info->sweep_samples = sw_n;
-        info->pad_ = 0;
+        info->sweep_variant = sw_variant;
         info->kernel_launches = extra_launches + cg_launches;
     }
     if (nonfinite) {
@@ -575,7 +671,7 @@ static int check_opts(const h3d_solve_opts *o)
     if (!o) return H3D_OK;
     if (!(o->tol > 0) || o->maxit < 1 || !(o->w > 0 && o->w < 2) ||
         (o->precision != H3D_PREC_FP64 && o->precision != H3D_PREC_MIXED) || o->order < 0 ||
-        o->order > 2 || (o->precision == H3D_PREC_MIXED && !(o->inner_tol > 0 && o->inner_tol < 1))) {
+        o->order > 3 || (o->method != H3D_METHOD_CGMN && o->method != H3D_METHOD_CRMN) || (o->precision == H3D_PREC_MIXED && !(o->inner_tol > 0 && o->inner_tol < 1))) {
         set_error("invalid solver options");
         return H3D_ERR_BAD_ARG;
     }

@@ -54,17 +54,21 @@ static int sweep_lex_pass(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrh
 template <typename T, bool ADJ, bool WNC>
 static int sweep_dispatch(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w,
                           int order, const int32_t *block, const int *active, cudaStream_t st,
-                          const T *rinv, int shape)
+                          const T *rinv, int shape, const cplx<T> *coef)
 {
     int rc = H3D_OK;
     if (order == H3D_ORDER_LEX) {
         rc = sweep_lex_pass<T, ADJ, WNC>(op, x, b, nrhs, w, active, false, st);
         if (!rc) rc = sweep_lex_pass<T, ADJ, WNC>(op, x, b, nrhs, w, active, true, st);
+    } else if (order == H3D_ORDER_COLOUR27 && coef && rinv) {
+        rc = sweep_colour_direct<T>(op, x, b, nrhs, w, active, rinv, coef, ADJ, st);
     } else if (order == H3D_ORDER_COLOUR27) {
         rc = sweep_colour_tiled<T>(op, x, b, nrhs, w, active, rinv, shape, ADJ, false, st);
         if (!rc) rc = sweep_colour_tiled<T>(op, x, b, nrhs, w, active, rinv, shape, ADJ, true, st);
     } else if (order == H3D_ORDER_BLOCK) {
-        rc = sweep_block(op, x, b, nrhs, w, block, active, ADJ, st);
+        rc = sweep_block(op, x, b, nrhs, w, block, active, ADJ, st, rinv, shape);
+    } else if (order == H3D_ORDER_BLOCK8) {
+        rc = sweep_block8(op, x, b, nrhs, w, block, active, ADJ, st, rinv, shape);
     } else {
         set_error("unknown sweep order %d", order);
         return H3D_ERR_BAD_ARG;
@@ -77,16 +81,16 @@ static int sweep_dispatch(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrh
 template <typename T>
 int launch_sweep(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, bool adj,
                  int order, const int32_t *block, const int *active, cudaStream_t st,
-                 const T *rinv, int shape)
+                 const T *rinv, int shape, const cplx<T> *coef)
 {
     const bool wnc = op.wni != nullptr;
-    if (!adj && !wnc) return sweep_dispatch<T, false, false>(op, x, b, nrhs, w, order, block, active, st, rinv, shape);
-    if (!adj && wnc) return sweep_dispatch<T, false, true>(op, x, b, nrhs, w, order, block, active, st, rinv, shape);
-    if (adj && !wnc) return sweep_dispatch<T, true, false>(op, x, b, nrhs, w, order, block, active, st, rinv, shape);
-    return sweep_dispatch<T, true, true>(op, x, b, nrhs, w, order, block, active, st, rinv, shape);
+    if (!adj && !wnc) return sweep_dispatch<T, false, false>(op, x, b, nrhs, w, order, block, active, st, rinv, shape, coef);
+    if (!adj && wnc) return sweep_dispatch<T, false, true>(op, x, b, nrhs, w, order, block, active, st, rinv, shape, coef);
+    if (adj && !wnc) return sweep_dispatch<T, true, false>(op, x, b, nrhs, w, order, block, active, st, rinv, shape, coef);
+    return sweep_dispatch<T, true, true>(op, x, b, nrhs, w, order, block, active, st, rinv, shape, coef);
 }
 
-template int launch_sweep<double>(const Op<double> &, cplx<double> *, const cplx<double> *, int, double, bool, int, const int32_t *, const int *, cudaStream_t, const double *, int);
-template int launch_sweep<float>(const Op<float> &, cplx<float> *, const cplx<float> *, int, float, bool, int, const int32_t *, const int *, cudaStream_t, const float *, int);
+template int launch_sweep<double>(const Op<double> &, cplx<double> *, const cplx<double> *, int, double, bool, int, const int32_t *, const int *, cudaStream_t, const double *, int, const cplx<double> *);
+template int launch_sweep<float>(const Op<float> &, cplx<float> *, const cplx<float> *, int, float, bool, int, const int32_t *, const int *, cudaStream_t, const float *, int, const cplx<float> *);
 
 }  // namespace h3d

@@ -55,8 +55,10 @@ constexpr size_t tile_smem()
     return sizeof(cplx<T>) * G::NBP + sizeof(T) * G::NBP * (WNC ? 2 : 1);
 }
 
-template <typename T, bool ADJ, bool WNC, int TU, int TV, int TW>
-__global__ void __launch_bounds__(TU *TV *TW, sizeof(T) == 4 ? 2 : 1) sweep_tile_kernel(Op<T> op, cplx<T> *x, const cplx<T> *b,
+// MINB: CTAs per SM the register allocation must allow (complex64: 2 caps a thread at 128
+// registers, 1 lets the 27 coefficients of a PML row stay in registers without spilling).
+template <typename T, bool ADJ, bool WNC, int TU, int TV, int TW, int MINB>
+__global__ void __launch_bounds__(TU *TV *TW, MINB) sweep_tile_kernel(Op<T> op, cplx<T> *x, const cplx<T> *b,
                                                                 int nrhs, int a, int bq, int cq, T w,
                                                                 const int *active, const T *rinv)
 {
@@ -108,14 +110,6 @@ __global__ void __launch_bounds__(TU *TV *TW, sizeof(T) == 4 ? 2 : 1) sweep_tile
                           rj1 < ihi[1] && cq + 3 * w0 >= ilo[2] && rk1 < ihi[2] && ri1 < op.nx &&
                           rj1 < op.ny && rk1 < op.nz;
 
-    RowPml<T> pml{};
-    uint32_t m = 0x7ffffffu;
-    T inv = T(0);
-    if (valid) {
-        pml = load_row_pml<T, ADJ>(op, i, j, k);
-        if (!ADJ) m = inside_mask(i, j, k, op.nx, op.ny, op.nz);
-        if (rinv) inv = rinv[ctr];
-    }
     cp_async_wait_all();
     __syncthreads();
 
@@ -124,64 +118,105 @@ __global__ void __launch_bounds__(TU *TV *TW, sizeof(T) == 4 ? 2 : 1) sweep_tile
         return mk<T>(swr[q], WNC ? swi[q] : T(0));
     };
     auto wnr = [&](int dx, int dy, int dz) { return swr[lc + dx + PX * (dy + BY * dz)]; };
-    if (valid && !rinv) {
-        // no precomputed norms: build them from the coefficients here
-        T nrm = T(0);
-        if (interior) {
-#define H3D_NI(t, dx, dy, dz) { const T cr = coef_int<t, dx, dy, dz, T, ADJ>(op, wnr); nrm += cr * cr; }
-            H3D_FOR_27(H3D_NI)
-#undef H3D_NI
-        } else {
-#define H3D_NG(t, dx, dy, dz) nrm += cabs2(coef_at<t, dx, dy, dz, T, ADJ, false, WNC>(op, pml, m, wnf));
-            H3D_FOR_27(H3D_NG)
-#undef H3D_NG
-        }
-        inv = T(1) / nrm;
-    }
-    const cplx<T> wc = valid ? wnf(0, 0, 0) : mk<T>(T(0), T(0));
 
-    for (int s = 0; s < nrhs; ++s) {
-        if (active && !active[s]) continue;  // uniform over the CTA
-        cplx<T> *xs = x + (long long)s * op.N;
-        if (s > 0) __syncthreads();  // the previous box is fully written back
-        for_box([&](int q, bool in, long long g) { cp_async_zfill<sizeof(cplx<T>)>(sx + q, xs + g, in); });
-        cp_async_wait_all();
-        __syncthreads();
-        if (valid) {
-            RowAcc<T> acc;
-            acc_zero(acc);
-            acc_plane<0, T, false>(acc, plane_sums<T, ADJ, WNC, PX>(sx, swr, swi, lc - PXY), op);
-            acc_plane<1, T, false>(acc, plane_sums<T, ADJ, WNC, PX>(sx, swr, swi, lc), op);
-            acc_plane<2, T, false>(acc, plane_sums<T, ADJ, WNC, PX>(sx, swr, swi, lc + PXY), op);
-            const cplx<T> atx = acc_finish<T, ADJ, false, WNC>(acc, pml, wc);
-            const cplx<T> bv = b ? b[(long long)s * op.N + ctr] : mk<T>(T(0), T(0));
+    // Per right-hand side: box in, project this thread's row (rows inside the grid only), box
+    // out.  The row's 27 coefficients are formed in registers right before its gather and
+    // reused by its scatter; they are formed again for every right-hand side, which keeps
+    // them out of the registers that live across the box copies (multi-RHS solves are
+    // better served by the BLOCK8 order, whose groups of right-hand sides share a block).
+    auto run_rhs = [&](auto &&project) {
+        for (int s = 0; s < nrhs; ++s) {
+            if (active && !active[s]) continue;  // uniform over the CTA
+            cplx<T> *xs = x + (long long)s * op.N;
+            if (s > 0) __syncthreads();  // the previous box is fully written back
+            for_box([&](int q, bool in, long long g) { cp_async_zfill<sizeof(cplx<T>)>(sx + q, xs + g, in); });
+            cp_async_wait_all();
+            __syncthreads();
+            if (valid) project(b ? b + (long long)s * op.N : nullptr);
+            __syncthreads();
+            for_box([&](int q, bool in, long long g) {
+                if (in) xs[g] = sx[q];
+            });
+        }
+    };
+
+    if (interior) {
+        // every row of the CTA has PML values of exactly 1: real coefficients K_t - WM_t wn
+        run_rhs([&](const cplx<T> *bs) {
+            T cr[27];
+#define H3D_CI(t, dx, dy, dz) cr[t] = coef_int<t, dx, dy, dz, T, ADJ>(op, wnr);
+            H3D_FOR_27(H3D_CI)
+#undef H3D_CI
+            T inv;
+            if (rinv) {
+                inv = rinv[ctr];
+            } else {
+                T nrm = T(0);
+#pragma unroll
+                for (int t = 0; t < 27; ++t) nrm += cr[t] * cr[t];
+                inv = T(1) / nrm;
+            }
+            // one partial sum per plane dz: three shorter dependency chains
+        cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+#define H3D_GI(t, dx, dy, dz)                                                                  \
+    {                                                                                          \
+        const cplx<T> xv = sx[lc + dx + PX * (dy + BY * dz)];                                  \
+        acc[dz + 1].re += cr[t] * xv.re;                                                       \
+        acc[dz + 1].im += cr[t] * xv.im;                                                       \
+    }
+            H3D_FOR_27(H3D_GI)
+#undef H3D_GI
+        const cplx<T> atx = (acc[0] + acc[1]) + acc[2];
+            const cplx<T> bv = bs ? bs[ctr] : mk<T>(T(0), T(0));
             const cplx<T> d = (w * inv) * (bv - atx);
-            if (interior) {
 #define H3D_SI(t, dx, dy, dz)                                                                  \
     {                                                                                          \
-        const T cr = coef_int<t, dx, dy, dz, T, ADJ>(op, wnr);                                 \
         cplx<T> &o = sx[lc + dx + PX * (dy + BY * dz)];                                        \
-        o.re += d.re * cr;                                                                     \
-        o.im += d.im * cr;                                                                     \
+        o.re += d.re * cr[t];                                                                  \
+        o.im += d.im * cr[t];                                                                  \
     }
-                H3D_FOR_27(H3D_SI)
+            H3D_FOR_27(H3D_SI)
 #undef H3D_SI
+        });
+    } else {
+        run_rhs([&](const cplx<T> *bs) {
+            const RowPml<T> pml = load_row_pml<T, ADJ>(op, i, j, k);
+            const uint32_t m = ADJ ? 0x7ffffffu : inside_mask(i, j, k, op.nx, op.ny, op.nz);
+            // forward coefficients of outside neighbours are zero; adjoint ones are not (they
+            // count in the norm), and x outside the grid is never stored (for_box)
+            cplx<T> c[27];
+#define H3D_CC(t, dx, dy, dz) c[t] = coef_at<t, dx, dy, dz, T, ADJ, false, WNC>(op, pml, m, wnf);
+            H3D_FOR_27(H3D_CC)
+#undef H3D_CC
+            T inv;
+            if (rinv) {
+                inv = rinv[ctr];
             } else {
+                T nrm = T(0);
+#pragma unroll
+                for (int t = 0; t < 27; ++t) nrm += cabs2(c[t]);
+                inv = T(1) / nrm;
+            }
+            cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+#define H3D_GC(t, dx, dy, dz)                                                                  \
+    {                                                                                          \
+        const cplx<T> xv = sx[lc + dx + PX * (dy + BY * dz)];                                  \
+        acc[dz + 1].re += c[t].re * xv.re - c[t].im * xv.im;                                   \
+        acc[dz + 1].im += c[t].re * xv.im + c[t].im * xv.re;                                   \
+    }
+            H3D_FOR_27(H3D_GC)
+#undef H3D_GC
+        const cplx<T> atx = (acc[0] + acc[1]) + acc[2];
+            const cplx<T> bv = bs ? bs[ctr] : mk<T>(T(0), T(0));
+            const cplx<T> d = (w * inv) * (bv - atx);
 #define H3D_SC(t, dx, dy, dz)                                                                  \
     {                                                                                          \
-        const cplx<T> cc = coef_at<t, dx, dy, dz, T, ADJ, false, WNC>(op, pml, m, wnf);        \
         cplx<T> &o = sx[lc + dx + PX * (dy + BY * dz)];                                        \
-        const cplx<T> u = d * cconj(cc);                                                       \
-        o.re += u.re;                                                                          \
-        o.im += u.im;                                                                          \
+        o.re += d.re * c[t].re + d.im * c[t].im;                                               \
+        o.im += d.im * c[t].re - d.re * c[t].im;                                               \
     }
-                H3D_FOR_27(H3D_SC)
+            H3D_FOR_27(H3D_SC)
 #undef H3D_SC
-            }
-        }
-        __syncthreads();
-        for_box([&](int q, bool in, long long g) {
-            if (in) xs[g] = sx[q];
         });
     }
 }
@@ -218,10 +253,10 @@ int row_inv_norms(const Op<T> &op, bool adj, T *rinv, cudaStream_t st)
 
 // Candidate tile shapes (rows of one colour per CTA).
 struct Shape {
-    int tu, tv, tw;
+    int tu, tv, tw, minb;
 };
-static const Shape kShapes[] = {{32, 4, 2}, {16, 8, 2}, {8, 8, 4}};
-constexpr int kNumShapes = 3;
+static const Shape kShapes[] = {{32, 4, 2, 2}, {16, 8, 2, 2}, {8, 8, 4, 2}, {32, 4, 2, 1}};
+constexpr int kNumShapes = 4;
 
 int num_tile_shapes() { return kNumShapes; }
 
@@ -231,7 +266,7 @@ int pick_tile_shape(int nx, int ny, int nz)
 {
     int best = 0;
     double best_eff = -1;
-    for (int s = 0; s < kNumShapes; ++s) {
+    for (int s = 0; s < 3; ++s) {  // the register-rich variant is left to the measured tuner
         double eff = 0;
         for (int q = 0; q < 27; ++q) {
             const int a = q % 3, b = (q / 3) % 3, c = q / 9;
@@ -250,14 +285,14 @@ int pick_tile_shape(int nx, int ny, int nz)
     return best;
 }
 
-template <typename T, bool ADJ, bool WNC, int TU, int TV, int TW>
+template <typename T, bool ADJ, bool WNC, int TU, int TV, int TW, int MINB>
 static int tile_pass_shape(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w,
                            const int *active, const T *rinv, bool backward, cudaStream_t st)
 {
     constexpr size_t smem = tile_smem<T, WNC, TU, TV, TW>();
     static bool attr_set = false;  // per template instance and process
     if (!attr_set) {
-        H3D_CUDA_TRY(cudaFuncSetAttribute(sweep_tile_kernel<T, ADJ, WNC, TU, TV, TW>,
+        H3D_CUDA_TRY(cudaFuncSetAttribute(sweep_tile_kernel<T, ADJ, WNC, TU, TV, TW, MINB>,
                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
         attr_set = true;
     }
@@ -268,7 +303,7 @@ static int tile_pass_shape(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nr
         const int nu = (op.nx - a + 2) / 3, nv = (op.ny - bq + 2) / 3, nw = (op.nz - cq + 2) / 3;
         if (nu <= 0 || nv <= 0 || nw <= 0) continue;
         const dim3 grd((nu + TU - 1) / TU, (nv + TV - 1) / TV, (nw + TW - 1) / TW);
-        sweep_tile_kernel<T, ADJ, WNC, TU, TV, TW><<<grd, blk, smem, st>>>(op, x, b, nrhs, a, bq, cq, w,
+        sweep_tile_kernel<T, ADJ, WNC, TU, TV, TW, MINB><<<grd, blk, smem, st>>>(op, x, b, nrhs, a, bq, cq, w,
                                                                           active, rinv);
     }
     H3D_CUDA_TRY(cudaGetLastError());
@@ -280,9 +315,10 @@ static int tile_pass(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T 
                      const int *active, const T *rinv, int shape, bool backward, cudaStream_t st)
 {
     switch (shape) {
-    case 1: return tile_pass_shape<T, ADJ, WNC, 16, 8, 2>(op, x, b, nrhs, w, active, rinv, backward, st);
-    case 2: return tile_pass_shape<T, ADJ, WNC, 8, 8, 4>(op, x, b, nrhs, w, active, rinv, backward, st);
-    default: return tile_pass_shape<T, ADJ, WNC, 32, 4, 2>(op, x, b, nrhs, w, active, rinv, backward, st);
+    case 1: return tile_pass_shape<T, ADJ, WNC, 16, 8, 2, sizeof(T) == 4 ? 2 : 1>(op, x, b, nrhs, w, active, rinv, backward, st);
+    case 2: return tile_pass_shape<T, ADJ, WNC, 8, 8, 4, sizeof(T) == 4 ? 2 : 1>(op, x, b, nrhs, w, active, rinv, backward, st);
+    case 3: return tile_pass_shape<T, ADJ, WNC, 32, 4, 2, 1>(op, x, b, nrhs, w, active, rinv, backward, st);
+    default: return tile_pass_shape<T, ADJ, WNC, 32, 4, 2, sizeof(T) == 4 ? 2 : 1>(op, x, b, nrhs, w, active, rinv, backward, st);
     }
 }
 

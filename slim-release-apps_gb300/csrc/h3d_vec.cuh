@@ -33,6 +33,11 @@ struct DevBuf {
         }
         return H3D_OK;
     }
+    void release()
+    {
+        if (p) cudaFreeAsync(p, st);
+        p = nullptr;
+    }
     template <typename U>
     U *as() const { return static_cast<U *>(p); }
 };

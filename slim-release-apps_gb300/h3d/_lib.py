@@ -19,7 +19,8 @@ ERR_NSIZE, ERR_XSIZE, ERR_BSIZE, ERR_BAD_ARG, ERR_NOT_CONVERGED, ERR_TIMEOUT, ER
     ERR_NO_MEMORY, ERR_NONFINITE = range(1, 10)
 C128, C64 = 0, 1
 FORWARD, ADJOINT = 1, 2
-ORDER_LEX, ORDER_COLOUR27, ORDER_BLOCK = 0, 1, 2
+ORDER_LEX, ORDER_COLOUR27, ORDER_BLOCK, ORDER_BLOCK8 = 0, 1, 2, 3
+METHOD_CGMN, METHOD_CRMN = 0, 1
 PREC_FP64, PREC_MIXED = 0, 1
 STOP_PRECONDITIONED, STOP_TRUE_RESIDUAL = 0, 1
 
@@ -33,7 +34,7 @@ class SolveOpts(C.Structure):
         ("tol", C.c_double), ("maxit", C.c_int32), ("w", C.c_double), ("precision", C.c_int32),
         ("order", C.c_int32), ("stop_rule", C.c_int32), ("check_every", C.c_int32),
         ("inner_tol", C.c_double), ("max_outer", C.c_int32), ("block", C.c_int32 * 3),
-        ("use_graphs", C.c_int32), ("verbose", C.c_int32),
+        ("use_graphs", C.c_int32), ("verbose", C.c_int32), ("method", C.c_int32),
     ]
 
 
@@ -41,12 +42,12 @@ class SolveInfo(C.Structure):
     _fields_ = [
         ("iters", C.c_int32), ("outer", C.c_int32), ("converged", C.c_int32), ("nrhs", C.c_int32),
         ("rel_res_true", C.c_double), ("rel_res_prec", C.c_double), ("seconds", C.c_double),
-        ("sweep_seconds", C.c_double), ("sweep_samples", C.c_int32), ("pad_", C.c_int32),
+        ("sweep_seconds", C.c_double), ("sweep_samples", C.c_int32), ("sweep_variant", C.c_int32),
         ("kernel_launches", C.c_int64),
     ]
 
     def as_dict(self):
-        return {k: getattr(self, k) for k, _ in self._fields_ if k != "pad_"}
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class Problem(C.Structure):

@@ -22,7 +22,7 @@ import torch
 from . import _lib as L
 
 _ORDERS = {"lex": L.ORDER_LEX, "colour27": L.ORDER_COLOUR27, "color27": L.ORDER_COLOUR27,
-           "block": L.ORDER_BLOCK}
+           "block": L.ORDER_BLOCK, "block8": L.ORDER_BLOCK8}
 
 
 def _grid(grid):
@@ -37,7 +37,7 @@ def _mode(mode) -> int:
 
 def make_opts(tol=1e-6, maxit=10000, precision="fp64", order="colour27", stop="true",
               inner_tol=None, max_outer=None, check_every=None, block=None, w=1.5,
-              use_graphs=True, verbose=False) -> L.SolveOpts:
+              use_graphs=True, verbose=False, method="cgmn") -> L.SolveOpts:
     o = L.default_opts()
     o.tol = float(tol)
     o.maxit = int(maxit)
@@ -56,6 +56,7 @@ def make_opts(tol=1e-6, maxit=10000, precision="fp64", order="colour27", stop="t
             o.block[a] = int(block[a])
     o.use_graphs = 1 if use_graphs else 0
     o.verbose = 1 if verbose else 0
+    o.method = {"cgmn": L.METHOD_CGMN, "crmn": L.METHOD_CRMN}[method] if isinstance(method, str) else int(method)
     return o
 
 

@@ -65,7 +65,7 @@ def test_adjoint_dot_product():
         assert abs(a - b) <= 1e-13 * abs(a)
 
 
-@pytest.mark.parametrize("order", [O.ORDER_LEX, O.ORDER_COLOUR27, O.ORDER_BLOCK])
+@pytest.mark.parametrize("order", [O.ORDER_LEX, O.ORDER_COLOUR27, O.ORDER_BLOCK, O.ORDER_BLOCK8])
 def test_double_sweep_symmetric_psd(order):
     """test_DoubleKaczmarzSweep.m:125-199 properties for every ordering: with
     Q y = DSWP(y, 0), the operator I - Q is Hermitian and positive semi-definite."""
@@ -97,8 +97,12 @@ def test_colour_orders_differ_from_lex_but_block_whole_grid_is_colour27():
     x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
     c27 = O.sweep(g, wn, 1.5, x, None, order=O.ORDER_COLOUR27, nthreads=1)
     blk = O.sweep(g, wn, 1.5, x, None, order=O.ORDER_BLOCK, blk=(6, 6, 6), nthreads=1)
+    blk8 = O.sweep(g, wn, 1.5, x, None, order=O.ORDER_BLOCK8, blk=(6, 6, 6), nthreads=1)
     lex = O.sweep(g, wn, 1.5, x, None, order=O.ORDER_LEX, nthreads=1)
     assert np.allclose(c27, blk, rtol=0, atol=1e-14 * np.abs(c27).max())
+    assert np.allclose(c27, blk8, rtol=0, atol=1e-14 * np.abs(c27).max())
+    blk8b = O.sweep(g, wn, 1.5, x, None, order=O.ORDER_BLOCK8, blk=(3, 3, 3), nthreads=1)
+    assert not np.allclose(c27, blk8b)
     assert not np.allclose(c27, lex)
 
 

@@ -2,7 +2,7 @@
 
 * LEX order + the reference stopping rule reproduces the reference iteration
   (linearsolve.m + CGMN.m): same iteration count and the same iterate to rounding.
-* COLOUR27 / BLOCK orders and the mixed-precision path converge to the same solution;
+* COLOUR27 / BLOCK / BLOCK8 orders and the mixed-precision path converge to the same solution;
   their true residual ||b - H u|| / ||b|| is checked in FP64 by the oracle matvec.
 """
 import numpy as np
@@ -44,35 +44,35 @@ def test_lex_cgmn_reproduces_reference_iteration(cuda, mode):
     assert np.linalg.norm(u - xref) / np.linalg.norm(xref) <= 1e-7
 
 
-@pytest.mark.parametrize("order", ["colour27", "block"])
+@pytest.mark.parametrize("order", ["colour27", "block", "block8"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 def test_reordered_and_mixed_solves_converge_to_reference_solution(cuda, order, precision):
     from h3d import solver
 
     grid, g, wn, b = _problem()
     xref = slim_ref.cgmn_solve(g, wn, b, tol=1e-11, maxit=6000, order=O.ORDER_COLOUR27)
-    u, info = solver.solve(grid, _t(wn, cuda), _t(b, cuda), tol=1e-6, order=order, block=(5, 5, 5),
-                           precision=precision)
+    u, info = solver.solve(grid, _t(wn, cuda), _t(b, cuda), tol=1e-6, order=order,
+                           block=(8, 8, 8) if order == "block" else None, precision=precision)
     u = u.cpu().numpy()
     tr = slim_ref.true_residual(g, wn, b, u)
     assert tr <= 1e-6 and info["rel_res_true"] <= 1e-6 and info["converged"] == 1
     assert np.linalg.norm(u - xref) / np.linalg.norm(xref) <= 1e-4
 
 
-def test_multi_rhs_masks_and_zero_rhs(cuda):
-    import torch
+@pytest.mark.parametrize("order", ["colour27", "block8"])
+def test_multi_rhs_masks_and_zero_rhs(cuda, order):
     from h3d import solver
 
     grid, g, wn, b = _problem(seed=2)
     N = b.size
     rng = np.random.default_rng(1)
     B = np.stack([b, np.zeros(N), rng.standard_normal(N) + 1j * rng.standard_normal(N)])
-    u, info = solver.solve(grid, _t(wn, cuda), _t(B, cuda), tol=1e-6, precision="fp64")
+    u, info = solver.solve(grid, _t(wn, cuda), _t(B, cuda), tol=1e-6, precision="fp64", order=order)
     u = u.cpu().numpy()
     assert np.all(u[1] == 0)                       # opAbstractMatrix.m:118
     for s in (0, 2):
         assert slim_ref.true_residual(g, wn, B[s], u[s]) <= 1e-6
-    u2, _ = solver.solve(grid, _t(wn, cuda), _t(B[2], cuda), tol=1e-6, precision="fp64")
+    u2, _ = solver.solve(grid, _t(wn, cuda), _t(B[2], cuda), tol=1e-6, precision="fp64", order=order)
     assert np.linalg.norm(u2.cpu().numpy() - u[2]) <= 1e-5 * np.linalg.norm(u[2])
 
 
@@ -101,3 +101,35 @@ def test_not_converged_reports_status(cuda):
     u, info = solver.solve(grid, _t(wn, cuda), _t(b, cuda), tol=1e-6, maxit=3, precision="fp64",
                            raise_not_converged=False)
     assert info["converged"] == 0 and info["iters"] == 3
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_lex_crmn_reproduces_reference_iteration(cuda, mode):
+    """LinSolveOpts.SOLVE_CRMN (CRMN.m through linearsolve.m:51-64) in the reference row order
+    and stopping rule: the same iteration count and iterate as the oracle restatement."""
+    from h3d import solver
+
+    grid, g, wn, b = _problem()
+    xref, hst = slim_ref.linearsolve_crmn(g, wn, b, mode=mode, tol=1e-6, maxit=3000, order=O.ORDER_LEX)
+    u, info = solver.solve(grid, _t(wn, cuda), _t(b, cuda), mode=mode, tol=1e-6, maxit=3000,
+                           order="lex", stop="preconditioned", precision="fp64", check_every=5,
+                           method="crmn")
+    assert abs(info["iters"] - (len(hst) - 1)) <= 1
+    u = u.cpu().numpy()
+    assert np.linalg.norm(u - xref) / np.linalg.norm(xref) <= 1e-7
+
+
+@pytest.mark.parametrize("order,precision", [("colour27", "fp64"), ("block8", "mixed")])
+def test_crmn_converges_on_true_residual(cuda, order, precision):
+    from h3d import solver
+
+    grid, g, wn, b = _problem(seed=4)
+    N = b.size
+    rng = np.random.default_rng(6)
+    B = np.stack([b, np.zeros(N), rng.standard_normal(N) + 1j * rng.standard_normal(N)])
+    u, info = solver.solve(grid, _t(wn, cuda), _t(B, cuda), tol=1e-6, order=order, precision=precision,
+                           method="crmn")
+    u = u.cpu().numpy()
+    assert info["converged"] == 1 and np.all(u[1] == 0)
+    for s in (0, 2):
+        assert slim_ref.true_residual(g, wn, B[s], u[s]) <= 1e-6

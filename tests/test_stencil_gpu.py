@@ -86,7 +86,9 @@ def test_lex_sweep_matches_reference(cuda, golden_small, tag):
         assert _rel(y.cpu().numpy().T, gs[f"{tag}/{key}"]) <= 1e-12, key
 
 
-@pytest.mark.parametrize("order,blk", [(1, None), (2, (3, 4, 3)), (2, (5, 5, 5))])
+# COLOUR27 twice: on stored row coefficients (block None) and with the shared-memory tile
+# kernel (block[0] = -1)
+@pytest.mark.parametrize("order,blk", [(1, None), (1, (-1, 0, 0)), (2, (8, 8, 8)), (2, (16, 8, 8))])
 @pytest.mark.parametrize("mode", [1, 2])
 def test_reordered_sweeps_match_oracle(cuda, golden_small, order, blk, mode):
     import torch
@@ -95,7 +97,7 @@ def test_reordered_sweeps_match_oracle(cuda, golden_small, order, blk, mode):
     gs, tag = golden_small, "g12"
     g = O.make_grid(gs[f"{tag}/n"].astype(int), gs[f"{tag}/h"], gs[f"{tag}/npml"].T.reshape(-1))
     X, B, wn = gs[f"{tag}/X"], gs[f"{tag}/B"], gs[f"{tag}/wn"]
-    ref = O.sweep(g, wn, 1.5, X, B, adj=(mode == 2), order=order, blk=blk, nthreads=2)
+    ref = O.sweep(g, wn, 1.5, X, B, adj=(mode == 2), order=order, blk=None if order == 1 else blk, nthreads=2)
     y = ops.kacz_sweep(_grid_args(gs, tag), _t(wn, cuda), 1.5, _t(X.T, cuda, torch.complex128),
                        _t(B.T, cuda, torch.complex128), mode, order=order, block=blk)
     assert _rel(y.cpu().numpy().T, ref) <= 1e-12
@@ -103,6 +105,35 @@ def test_reordered_sweeps_match_oracle(cuda, golden_small, order, blk, mode):
     y32 = ops.kacz_sweep(_grid_args(gs, tag), _t(wn.astype(np.float32), cuda), 1.5,
                          _t(X.T, cuda, torch.complex64), _t(B.T, cuda, torch.complex64), mode,
                          order=order, block=blk)
+    assert _rel(y32.cpu().numpy().T.astype(np.complex128), ref) <= 5e-5
+
+
+@pytest.mark.parametrize("order,blk", [(3, (12, 12, 12)), (3, (24, 12, 12)), (1, None), (1, (-1, 0, 0))])
+@pytest.mark.parametrize("mode,wnc", [(1, False), (2, False), (1, True), (2, True)])
+def test_block8_and_colour27_sweeps_match_oracle(cuda, order, blk, mode, wnc):
+    """BLOCK8 (parity classes of blocks) on a grid of several blocks per axis and COLOUR27
+    (stored coefficients / tile kernel), three right-hand sides (a partly filled group of
+    two for BLOCK8 12^3), real and complex wavenumber, against the C oracle."""
+    import torch
+    from h3d import ops
+
+    n, h, npml = (29, 27, 26), (25.0, 22.0, 20.0), (3, 4, 2, 3, 4, 2)
+    rng = np.random.default_rng(31)
+    N = int(np.prod(n))
+    g = O.make_grid(n, h, npml)
+    wn = (2 * np.pi * 5.0) ** 2 / (1500.0 + 1500.0 * rng.random(N)) ** 2
+    if wnc:
+        wn = wn * (1.0 + 0.05j * rng.random(N))
+    X = rng.standard_normal((N, 3)) + 1j * rng.standard_normal((N, 3))
+    B = rng.standard_normal((N, 3)) + 1j * rng.standard_normal((N, 3))
+    ref = O.sweep(g, wn, 1.5, X, B, adj=(mode == 2), order=order, blk=blk if order == 3 else None, nthreads=2)
+    grid = (n, h, npml)
+    y = ops.kacz_sweep(grid, _t(wn, cuda), 1.5, _t(X.T, cuda, torch.complex128), _t(B.T, cuda, torch.complex128),
+                       mode, order=order, block=blk)
+    assert _rel(y.cpu().numpy().T, ref) <= 1e-12
+    wn32 = wn.astype(np.complex64) if wnc else wn.astype(np.float32)
+    y32 = ops.kacz_sweep(grid, _t(wn32, cuda), 1.5, _t(X.T, cuda, torch.complex64), _t(B.T, cuda, torch.complex64),
+                         mode, order=order, block=blk)
     assert _rel(y32.cpu().numpy().T.astype(np.complex128), ref) <= 5e-5
 
 
