@@ -156,9 +156,10 @@ int h3d_mvp(const h3d_grid *g, const void *wn_re, const void *wn_im, const void 
 
 /* One forward + backward Kaczmarz sweep with relaxation w on x (in place), right-hand
  * side b (NULL = 0).  Same element types as h3d_mvp.  block: BLOCK / BLOCK8 block size
- * (NULL or 0 = default); for COLOUR27, block[0] == -1 selects the shared-memory tile
- * kernel instead of the kernel on stored row coefficients (27 N complex values of
- * temporary device memory; used whenever they fit). */
+ * (NULL or 0 = default).  COLOUR27 and BLOCK8 with 12x12x12 blocks run on stored row
+ * coefficients (about 27 N complex values of temporary device memory) whenever they fit;
+ * block[0] == -1 selects the kernels that form the coefficients themselves (COLOUR27: the
+ * shared-memory tile kernel; BLOCK8: 12x12x12 blocks). */
 int h3d_kacz_sweep(const h3d_grid *g, const void *wn_re, const void *wn_im, double w, void *x,
                    const void *b, int nrhs, int mode, int order, const int32_t *block, int dtype,
                    void *stream);

@@ -68,8 +68,9 @@ __global__ void __launch_bounds__(kBlockThreads) sweep_block_smem_kernel(
             if (!(act & (1u << r))) continue;
             const int i = fi + 3 * (row % nu), j = fj + 3 * ((row / nu) % nv), k = fk + 3 * (row / (nu * nv));
             const int lc = (i - i0) + PX * ((j - j0) + PY * (k - k0));
-            block_row<T, ADJ, WNC, PX, PY>(op, sx + (size_t)r * NB, swr, swi,
-                                           b ? b + (long long)(s0 + r) * op.N : nullptr, rinv, w, i, j, k, lc);
+            const long long ctr = i + op.sy * j + op.sz * k;
+            const cplx<T> bv = b ? b[(long long)(s0 + r) * op.N + ctr] : mk<T>(T(0), T(0));
+            block_row<T, ADJ, WNC, PX, PY>(op, sx + (size_t)r * NB, swr, swi, bv, rinv[ctr], w, i, j, k, lc);
         }
         __syncthreads();
     }

@@ -15,25 +15,66 @@
 // and a pass is 8 launches.  With block sides divisible by 3 every colour has the same
 // (BX/3)(BY/3)(BZ/3) rows in a block (fewer at the grid's far faces), so thread t owns one
 // fixed (row, right-hand side) slot for all colours: no index division in the colour loop.
+//
+// Stored coefficients (12x12x12 blocks): the 27 coefficients of every row are formed once
+// per operator (coef8_store_kernel) and kept block- and colour-major, so the coefficients of
+// one colour of one block are one contiguous slab of 27 x 64 values (13.8 KB complex64).
+// A block that is not entirely interior copies the next colour's slab into shared memory
+// (cp.async, double-buffered) while it projects the current colour, and its rows read their
+// coefficients from there instead of forming complex PML expressions; interior blocks keep
+// forming their real coefficients from the wavenumber.
 #include "h3d_blockrow.cuh"
 #include "h3d_kernels.cuh"
 #include "h3d_vec.cuh"
 
 namespace h3d {
 
+// Stored-coefficient layout of BXxBYxBZ blocks: slab (block bid, colour q) starts at
+// (bid * 27 + q) * 27 * NR; coefficient t of row r = u + U (w + W v) of the slab at
+// + t * NR + r (the kernel's thread order).
+template <int BX, int BY, int BZ>
+struct Coef8Layout {
+    static constexpr int U = BX / 3, V = BY / 3, W = BZ / 3, NR = U * V * W;
+    static constexpr int SLAB = 27 * NR;  // complex values per (block, colour)
+};
+
+template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ>
+__global__ void __launch_bounds__(128) coef8_store_kernel(Op<T> op, cplx<T> *coef, int NI, int NJ)
+{
+    using L = Coef8Layout<BX, BY, BZ>;
+    const int bq = blockIdx.x;  // block * 27 + colour
+    const int bid = bq / 27, q = bq % 27;
+    const int Ib = bid % NI, Jb = (bid / NI) % NJ, Kb = bid / (NI * NJ);
+    const int a = q % 3, b = (q / 3) % 3, c = q / 9;
+    for (int row = threadIdx.x; row < L::NR; row += blockDim.x) {
+        const int u = row % L::U, w = (row / L::U) % L::W, v = row / (L::U * L::W);
+        const int i = Ib * BX + a + 3 * u, j = Jb * BY + b + 3 * v, k = Kb * BZ + c + 3 * w;
+        if (i >= op.nx || j >= op.ny || k >= op.nz) continue;
+        const uint32_t m = ADJ ? 0x7ffffffu : inside_mask(i, j, k, op.nx, op.ny, op.nz);
+        cplx<T> cc[27];
+        row_coefs<T, ADJ, false, WNC>(op, i, j, k, m, cc);
+        cplx<T> *dst = coef + (size_t)bq * L::SLAB + row;
+#pragma unroll
+        for (int t = 0; t < 27; ++t) dst[t * L::NR] = cc[t];
+    }
+}
+
 template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ, int R>
 __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_block8_kernel(
     Op<T> op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active, const T *rinv,
-    int NIp, int NJp, int par, int backward)
+    const cplx<T> *coef, int NI, int NJ, int NIp, int NJp, int par, int backward)
 {
     static_assert(BX % 3 == 0 && BY % 3 == 0 && BZ % 3 == 0, "block sides must be multiples of 3");
     constexpr int U = BX / 3, V = BY / 3, W = BZ / 3, NR = U * V * W, NT = NR * R;
+    constexpr int SLAB = 27 * NR;
     using G = BlockGeom<BX, BY, BZ>;
     constexpr int PX = G::PX, PY = G::PY, NB = G::NB;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     cplx<T> *sx = reinterpret_cast<cplx<T> *>(smem_raw);  // [R][NB]
     T *swr = reinterpret_cast<T *>(sx + (size_t)R * NB);
     T *swi = WNC ? swr + NB : nullptr;
+    // [2][SLAB] staged coefficients, after the wavenumber box (16-byte aligned)
+    cplx<T> *sc = reinterpret_cast<cplx<T> *>(smem_raw + ((block_smem<T, WNC, BX, BY, BZ, R>() + 15) / 16) * 16);
 
     const int bid = blockIdx.x;
     const int Ib = (par & 1) + 2 * (bid % NIp);
@@ -51,23 +92,70 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_bloc
         if (s0 + r < nrhs && (!active || active[s0 + r])) act |= 1u << r;
     if (!act) return;
 
+    // every row of the block has PML values of exactly 1 (CTA-uniform)
+    const int *ilo = ADJ ? op.int_lo_a : op.int_lo_f, *ihi = ADJ ? op.int_hi_a : op.int_hi_f;
+    const bool interior_block = !WNC && bi0 >= ilo[0] && min(bi0 + BX, op.nx) <= ihi[0] && bj0 >= ilo[1] &&
+                                min(bj0 + BY, op.ny) <= ihi[1] && bk0 >= ilo[2] && min(bk0 + BZ, op.nz) <= ihi[2];
+    const bool stored = coef != nullptr && !interior_block;
+    const cplx<T> *slab0 = stored ? coef + (size_t)((Ib + NI * (Jb + NJ * Kb)) * 27) * SLAB : nullptr;
+    auto stage = [&](int q, int buf) {  // colour q's slab -> sc[buf], 16-byte copies
+        constexpr int CH = SLAB * (int)sizeof(cplx<T>) / 16;
+        const char *src = reinterpret_cast<const char *>(slab0 + (size_t)q * SLAB);
+        char *dst = reinterpret_cast<char *>(sc + buf * SLAB);
+        for (int e = threadIdx.x; e < CH; e += NT) blk_cp_async<16>(dst + 16 * e, src + 16 * e, true);
+    };
+
     block_stage<T, WNC, PX, PY, NB, R, NT>(op, x, s0, act, i0, j0, k0, sx, swr, swi);
+    if (stored) {
+        stage(backward ? 26 : 0, 0);
+        asm volatile("cp.async.commit_group;\n" ::: "memory");
+        asm volatile("cp.async.wait_group 0;\n" ::: "memory");
+    }
     __syncthreads();
 
-    // this thread's slot: row (u, v, w) of every colour, right-hand side s0 + r
+    // this thread's slot: row (u, v, w) of every colour, right-hand side s0 + r.  u, then w,
+    // then v: a half-warp spans (u, w), whose box offsets 3u + 3 PX PY w hit 16 distinct
+    // 8-byte bank pairs for the 14-point box pitch (no shared-memory bank conflicts).
     const int tid = threadIdx.x;
     const int r = tid / NR, row = tid % NR;
-    const int u = row % U, v = (row / U) % V, ww = row / (U * V);
+    const int u = row % U, ww = (row / U) % W, v = row / (U * W);
     const bool mine = (act >> r) & 1u;
     cplx<T> *bx = sx + (size_t)r * NB;
     const cplx<T> *bs = b ? b + (long long)(s0 + r) * op.N : nullptr;
+    // b_i and 1/||a_i||^2 of the next colour's row are fetched one colour step ahead, so
+    // their global-memory latency overlaps the current step
+    T inv_n = T(0);
+    cplx<T> bv_n = mk<T>(T(0), T(0));
+    auto fetch = [&](int q) {
+        const int i = bi0 + q % 3 + 3 * u, j = bj0 + (q / 3) % 3 + 3 * v, k = bk0 + q / 9 + 3 * ww;
+        if (mine && i < op.nx && j < op.ny && k < op.nz) {
+            const long long ctr = i + op.sy * j + op.sz * k;
+            inv_n = rinv[ctr];
+            if (bs) bv_n = bs[ctr];
+        }
+    };
+    fetch(backward ? 26 : 0);
     for (int qq = 0; qq < 27; ++qq) {
         const int q = backward ? 26 - qq : qq;
+        const T inv = inv_n;
+        const cplx<T> bv = bv_n;
+        if (qq < 26) fetch(backward ? 25 - qq : qq + 1);
+        if (stored) {
+            // prefetch the next colour's coefficients into the other buffer (its previous
+            // colour finished at the barrier that ended the last iteration)
+            if (qq < 26) stage(backward ? 25 - qq : qq + 1, (qq + 1) & 1);
+            asm volatile("cp.async.commit_group;\n" ::: "memory");
+            asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this colour's slab landed
+            __syncthreads();
+        }
         const int a = q % 3, bq = (q / 3) % 3, cq = q / 9;
         const int i = bi0 + a + 3 * u, j = bj0 + bq + 3 * v, k = bk0 + cq + 3 * ww;
         if (mine && i < op.nx && j < op.ny && k < op.nz) {
             const int lc = (1 + a + 3 * u) + PX * ((1 + bq + 3 * v) + PY * (1 + cq + 3 * ww));
-            block_row<T, ADJ, WNC, PX, PY>(op, bx, swr, swi, bs, rinv, w, i, j, k, lc);
+            if (stored)
+                block_row_stored<T, PX, PY>(op, bx, sc + (qq & 1) * SLAB, NR, row, bv, inv, w, i, j, k, lc);
+            else
+                block_row<T, ADJ, WNC, PX, PY>(op, bx, swr, swi, bv, inv, w, i, j, k, lc);
         }
         __syncthreads();
     }
@@ -101,18 +189,23 @@ void block8_cfg_dims(int c, int32_t *blk, int *r)
 
 template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ, int R>
 static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active,
-                         const T *rinv, bool backward, cudaStream_t st)
+                         const T *rinv, const cplx<T> *coef, bool backward, cudaStream_t st)
 {
-    constexpr size_t smem = block_smem<T, WNC, BX, BY, BZ, R>();
+    constexpr size_t smem_box = block_smem<T, WNC, BX, BY, BZ, R>();
+    constexpr size_t smem_coef = ((smem_box + 15) / 16) * 16 + 2 * sizeof(cplx<T>) * Coef8Layout<BX, BY, BZ>::SLAB;
     constexpr int NT = (BX / 3) * (BY / 3) * (BZ / 3) * R;
-    if constexpr (smem > 232448) {  // 227 KB: the per-CTA shared-memory limit
+    if constexpr (smem_box > 232448) {  // 227 KB: the per-CTA shared-memory limit
         set_error("BLOCK8 configuration %dx%dx%d x %d right-hand sides exceeds shared memory", BX, BY, BZ, R);
         return H3D_ERR_BAD_ARG;
     } else {
+        // stored coefficients only where their double buffer fits next to the box
+        if (smem_coef > 232448) coef = nullptr;
+        const size_t smem = coef ? smem_coef : smem_box;
         static bool attr_set = false;  // per template instance and process
         if (!attr_set) {
+            const size_t mx = smem_coef > 232448 ? smem_box : smem_coef;
             H3D_CUDA_TRY(cudaFuncSetAttribute(sweep_block8_kernel<T, ADJ, WNC, BX, BY, BZ, R>,
-                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
             attr_set = true;
         }
         const int NI = (op.nx + BX - 1) / BX, NJ = (op.ny + BY - 1) / BY, NK = (op.nz + BZ - 1) / BZ;
@@ -131,8 +224,8 @@ static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs
         const dim3 grd((unsigned)nblk, ngrp);
         for (int pp = 0; pp < 8; ++pp) {
             const int par = backward ? 7 - pp : pp;
-            sweep_block8_kernel<T, ADJ, WNC, BX, BY, BZ, R>
-                <<<grd, NT, smem, st>>>(op, x, b, nrhs, w, active, rinv, NIp, NJp, par, backward ? 1 : 0);
+            sweep_block8_kernel<T, ADJ, WNC, BX, BY, BZ, R><<<grd, NT, smem, st>>>(
+                op, x, b, nrhs, w, active, rinv, coef, NI, NJ, NIp, NJp, par, backward ? 1 : 0);
         }
         H3D_CUDA_TRY(cudaGetLastError());
         return H3D_OK;
@@ -141,14 +234,39 @@ static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs
 
 template <typename T, bool ADJ, bool WNC>
 static int block8_pass_cfg(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active,
-                           const T *rinv, int cfg, bool backward, cudaStream_t st)
+                           const T *rinv, const cplx<T> *coef, int cfg, bool backward, cudaStream_t st)
 {
+    // the stored layout is the 12x12x12 one: the 24x12x12 configuration forms coefficients itself
     switch (cfg) {
-    case 1: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 2>(op, x, b, nrhs, w, active, rinv, backward, st);
-    case 2: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 4>(op, x, b, nrhs, w, active, rinv, backward, st);
-    case 3: return block8_pass_t<T, ADJ, WNC, 24, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, backward, st);
-    default: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, backward, st);
+    case 1: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 2>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
+    case 2: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 4>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
+    case 3: return block8_pass_t<T, ADJ, WNC, 24, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, nullptr, backward, st);
+    default: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
     }
+}
+
+size_t block8_coef_count(int nx, int ny, int nz)
+{
+    const size_t NI = (nx + 11) / 12, NJ = (ny + 11) / 12, NK = (nz + 11) / 12;
+    return NI * NJ * NK * 27 * Coef8Layout<12, 12, 12>::SLAB;
+}
+
+template <typename T>
+int store_block8_coefs(const Op<T> &op, bool adj, cplx<T> *coef, cudaStream_t st)
+{
+    const int NI = (op.nx + 11) / 12, NJ = (op.ny + 11) / 12, NK = (op.nz + 11) / 12;
+    const long long nbq = (long long)NI * NJ * NK * 27;
+    if (nbq > 0x7fffffffLL) {
+        set_error("grid too large for the BLOCK8 coefficient store");
+        return H3D_ERR_NSIZE;
+    }
+    const bool wnc = op.wni != nullptr;
+    if (!adj && !wnc) coef8_store_kernel<T, false, false, 12, 12, 12><<<(unsigned)nbq, 64, 0, st>>>(op, coef, NI, NJ);
+    else if (!adj && wnc) coef8_store_kernel<T, false, true, 12, 12, 12><<<(unsigned)nbq, 64, 0, st>>>(op, coef, NI, NJ);
+    else if (adj && !wnc) coef8_store_kernel<T, true, false, 12, 12, 12><<<(unsigned)nbq, 64, 0, st>>>(op, coef, NI, NJ);
+    else coef8_store_kernel<T, true, true, 12, 12, 12><<<(unsigned)nbq, 64, 0, st>>>(op, coef, NI, NJ);
+    H3D_CUDA_TRY(cudaGetLastError());
+    return H3D_OK;
 }
 
 // Configuration for an explicit block size: the matching shape with the largest group that
@@ -166,7 +284,7 @@ static int cfg8_for_block(const int32_t *blk, int nrhs)
 
 template <typename T>
 int sweep_block8(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int32_t *block,
-                 const int *active, bool adj, cudaStream_t st, const T *rinv, int cfg)
+                 const int *active, bool adj, cudaStream_t st, const T *rinv, int cfg, const cplx<T> *coef)
 {
     if (cfg < 0) {
         int32_t blk[3] = {12, 12, 12};
@@ -193,16 +311,18 @@ int sweep_block8(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, c
     for (int pass = 0; pass < 2; ++pass) {
         const bool bw = pass == 1;
         int rc;
-        if (!adj && !wnc) rc = block8_pass_cfg<T, false, false>(op, x, b, nrhs, w, active, rinv, cfg, bw, st);
-        else if (!adj && wnc) rc = block8_pass_cfg<T, false, true>(op, x, b, nrhs, w, active, rinv, cfg, bw, st);
-        else if (adj && !wnc) rc = block8_pass_cfg<T, true, false>(op, x, b, nrhs, w, active, rinv, cfg, bw, st);
-        else rc = block8_pass_cfg<T, true, true>(op, x, b, nrhs, w, active, rinv, cfg, bw, st);
+        if (!adj && !wnc) rc = block8_pass_cfg<T, false, false>(op, x, b, nrhs, w, active, rinv, coef, cfg, bw, st);
+        else if (!adj && wnc) rc = block8_pass_cfg<T, false, true>(op, x, b, nrhs, w, active, rinv, coef, cfg, bw, st);
+        else if (adj && !wnc) rc = block8_pass_cfg<T, true, false>(op, x, b, nrhs, w, active, rinv, coef, cfg, bw, st);
+        else rc = block8_pass_cfg<T, true, true>(op, x, b, nrhs, w, active, rinv, coef, cfg, bw, st);
         if (rc) return rc;
     }
     return H3D_OK;
 }
 
-template int sweep_block8<double>(const Op<double> &, cplx<double> *, const cplx<double> *, int, double, const int32_t *, const int *, bool, cudaStream_t, const double *, int);
-template int sweep_block8<float>(const Op<float> &, cplx<float> *, const cplx<float> *, int, float, const int32_t *, const int *, bool, cudaStream_t, const float *, int);
+template int sweep_block8<double>(const Op<double> &, cplx<double> *, const cplx<double> *, int, double, const int32_t *, const int *, bool, cudaStream_t, const double *, int, const cplx<double> *);
+template int sweep_block8<float>(const Op<float> &, cplx<float> *, const cplx<float> *, int, float, const int32_t *, const int *, bool, cudaStream_t, const float *, int, const cplx<float> *);
+template int store_block8_coefs<double>(const Op<double> &, bool, cplx<double> *, cudaStream_t);
+template int store_block8_coefs<float>(const Op<float> &, bool, cplx<float> *, cudaStream_t);
 
 }  // namespace h3d

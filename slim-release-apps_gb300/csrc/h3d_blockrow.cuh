@@ -40,7 +40,7 @@ struct BlockGeom {
 };
 
 template <typename T, bool WNC, int BX, int BY, int BZ, int R>
-constexpr size_t block_smem()
+__host__ __device__ constexpr size_t block_smem()
 {
     using G = BlockGeom<BX, BY, BZ>;
     return sizeof(cplx<T>) * G::NB * R + sizeof(T) * G::NB * (WNC ? 2 : 1);
@@ -84,18 +84,16 @@ __device__ __forceinline__ void block_store(const Op<T> &op, cplx<T> *x, int s0,
     }
 }
 
-// Project row (i, j, k) at box index lc for one right-hand side (box bx, right-hand side
-// value pointer bs = b + s N or null).  The 27 coefficients are formed once, in registers,
-// and serve both the gather (three partial sums, one per plane dz, each in offset order)
-// and the scatter.  Rows whose whole footprint has PML values of exactly 1 have real
+// Project row (i, j, k) at box index lc for one right-hand side (box bx; bv = b_i and
+// inv = 1/||a_i||^2, loaded by the caller so that it can fetch them ahead of time).  The 27
+// coefficients are formed once, in registers, and serve both the gather (three partial
+// sums, one per plane dz, each in offset order) and the scatter.  Rows whose whole footprint has PML values of exactly 1 have real
 // coefficients: K_t - WM_t wn.
 template <typename T, bool ADJ, bool WNC, int PX, int PY>
 __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T *swr, const T *swi,
-                                          const cplx<T> *bs, const T *rinv, T w, int i, int j, int k,
-                                          int lc)
+                                          cplx<T> bv, T inv, T w, int i, int j, int k, int lc)
 {
     const int *ilo = ADJ ? op.int_lo_a : op.int_lo_f, *ihi = ADJ ? op.int_hi_a : op.int_hi_f;
-    const long long ctr = i + op.sy * j + op.sz * k;
     const bool interior =
         !WNC && i >= ilo[0] && i < ihi[0] && j >= ilo[1] && j < ihi[1] && k >= ilo[2] && k < ihi[2];
     auto wnf = [&](int dx, int dy, int dz) {
@@ -103,8 +101,6 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
         return mk<T>(swr[qd], WNC ? swi[qd] : T(0));
     };
     auto wnr = [&](int dx, int dy, int dz) { return swr[lc + dx + PX * (dy + PY * dz)]; };
-    const T inv = rinv[ctr];
-    const cplx<T> bv = bs ? bs[ctr] : mk<T>(T(0), T(0));
     if (interior) {
         T cr[27];
 #define H3D_CI(t, dx, dy, dz) cr[t] = coef_int<t, dx, dy, dz, T, ADJ>(op, wnr);
@@ -159,6 +155,38 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
         H3D_FOR_27(H3D_SC)
 #undef H3D_SC
     }
+}
+
+// Project row (i, j, k) with its 27 coefficients read from shared memory (sc[t * NR + row],
+// staged from the stored coefficients).  Neighbours outside the grid are masked as above.
+template <typename T, int PX, int PY>
+__device__ __forceinline__ void block_row_stored(const Op<T> &op, cplx<T> *bx, const cplx<T> *sc, int NR, int row,
+                                                 cplx<T> bv, T inv, T w, int i, int j, int k, int lc)
+{
+    const bool edge = i == 0 || j == 0 || k == 0 || i == op.nx - 1 || j == op.ny - 1 || k == op.nz - 1;
+    const uint32_t m = edge ? inside_mask(i, j, k, op.nx, op.ny, op.nz) : 0x7ffffffu;
+    cplx<T> c[27];
+#pragma unroll
+    for (int t = 0; t < 27; ++t) c[t] = sc[t * NR + row];
+    cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+#define H3D_GS(t, dx, dy, dz)                                                                  \
+    {                                                                                          \
+        const cplx<T> xv = bx[lc + dx + PX * (dy + PY * dz)];                                  \
+        acc[dz + 1].re += c[t].re * xv.re - c[t].im * xv.im;                                   \
+        acc[dz + 1].im += c[t].re * xv.im + c[t].im * xv.re;                                   \
+    }
+    H3D_FOR_27(H3D_GS)
+#undef H3D_GS
+    const cplx<T> atx = (acc[0] + acc[1]) + acc[2];
+    const cplx<T> d = (w * inv) * (bv - atx);
+#define H3D_SS(t, dx, dy, dz)                                                                  \
+    if (m & (1u << t)) {                                                                       \
+        cplx<T> &o = bx[lc + dx + PX * (dy + PY * dz)];                                        \
+        o.re += d.re * c[t].re + d.im * c[t].im;                                               \
+        o.im += d.im * c[t].re - d.re * c[t].im;                                               \
+    }
+    H3D_FOR_27(H3D_SS)
+#undef H3D_SS
 }
 
 }  // namespace h3d

@@ -12,9 +12,10 @@ using namespace h3d;
 namespace h3d {
 const char *last_error();
 
-// COLOUR27 runs on stored row coefficients (formed here for this call) unless block[0] is
-// -1 or they do not fit in device memory; then the shared-memory tile kernel runs.  Both
-// give the COLOUR27 result to rounding.
+// COLOUR27 and BLOCK8 (12x12x12 blocks) run on stored row coefficients formed here for
+// this call, unless block[0] is -1 or they do not fit in device memory; then the kernels
+// that form the coefficients themselves run (COLOUR27: the shared-memory tile kernel).
+// Both give the same row order's result to rounding.
 template <typename T>
 static int kacz_sweep_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, bool adj, int order,
                         const int32_t *block, cudaStream_t st)
@@ -29,6 +30,16 @@ static int kacz_sweep_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs,
             return rc;
         }
         (void)cudaGetLastError();  // out of memory is not sticky: fall back to the tile kernel
+    }
+    const bool blk12 = !block || block[0] == 0 || (block[0] == 12 && block[1] == 12 && block[2] == 12);
+    if (order == H3D_ORDER_BLOCK8 && blk12) {
+        DevBuf cb;
+        if (cb.alloc(sizeof(cplx<T>) * block8_coef_count(op.nx, op.ny, op.nz), st) == H3D_OK) {
+            int rc = store_block8_coefs<T>(op, adj, cb.as<cplx<T>>(), st);
+            if (!rc) rc = launch_sweep<T>(op, x, b, nrhs, w, adj, order, block, nullptr, st, nullptr, -1, cb.as<cplx<T>>());
+            return rc;
+        }
+        (void)cudaGetLastError();
     }
     return launch_sweep<T>(op, x, b, nrhs, w, adj, order, block, nullptr, st);
 }

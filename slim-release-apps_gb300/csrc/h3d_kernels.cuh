@@ -68,10 +68,14 @@ size_t block_cfg_smem(int c, bool fp64, bool wnc);
 
 // h3d_block8.cu: the BLOCK8 ordering (eight parity classes of blocks, 27 colours inside a
 // block); cfg as for sweep_block (12x12x12 by default).
+// coef: stored coefficients in the 12x12x12 block layout (store_block8_coefs), or null.
 template <typename T>
 int sweep_block8(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w,
                  const int32_t *block, const int *active, bool adj, cudaStream_t st,
-                 const T *rinv = nullptr, int cfg = -1);
+                 const T *rinv = nullptr, int cfg = -1, const cplx<T> *coef = nullptr);
+size_t block8_coef_count(int nx, int ny, int nz);  // complex values of the stored layout
+template <typename T>
+int store_block8_coefs(const Op<T> &op, bool adj, cplx<T> *coef, cudaStream_t st);
 int num_block8_cfgs();
 void block8_cfg_dims(int c, int32_t *blk, int *r);
 size_t block8_cfg_smem(int c, bool fp64, bool wnc);

@@ -92,7 +92,7 @@ struct CgRun {
     cplx<T> *ap = nullptr;  // CRMN: A p
     T *rinv = nullptr;   // 1/||a_i||^2 per row, computed once (all orders but LEX)
     int shape = -1;      // COLOUR27 tile shape (num_tile_shapes(): stored coefficients), BLOCK cfg
-    cplx<T> *coef = nullptr;  // COLOUR27 stored row coefficients (27 N), when they fit
+    cplx<T> *coef = nullptr;  // stored row coefficients (COLOUR27: colour-major 27 N; BLOCK8: 12^3 block layout)
     CgState s{};
     DevBuf vecs, scal, ints, parts, norms, coefs;
     cudaGraphExec_t exec = nullptr;
@@ -177,6 +177,17 @@ struct CgRun {
             }
             (void)cudaGetLastError();
         }
+        const bool blk12 = block[0] <= 0 || (block[0] == 12 && block[1] == 12 && block[2] == 12);
+        if (order == H3D_ORDER_BLOCK8 && blk12) {
+            size_t fr = 0, tot = 0;
+            const size_t bytes = sizeof(cplx<T>) * block8_coef_count(op.nx, op.ny, op.nz);
+            if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && bytes <= fr / 2 && coefs.alloc(bytes, st) == H3D_OK) {
+                coef = coefs.as<cplx<T>>();
+                if ((rc = store_block8_coefs<T>(op, adj, coef, st))) return rc;
+                launches += 1;
+            }
+            (void)cudaGetLastError();
+        }
         return H3D_OK;
     }
 
@@ -239,7 +250,8 @@ struct CgRun {
                 // only groups the right-hand sides fill, and configurations that fit
                 if (r > nrhs || smem == 0) continue;
             }
-            const cplx<T> *cf = (order == H3D_ORDER_COLOUR27 && sh == num_tile_shapes()) ? coef : nullptr;
+            const cplx<T> *cf = (order == H3D_ORDER_COLOUR27 && sh == num_tile_shapes()) || order == H3D_ORDER_BLOCK8
+                                    ? coef : nullptr;
             if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, nullptr, st, rinv, sh, cf))) break;
             cudaEventRecord(e0, st);
             for (int rep = 0; rep < 2 && !rc; ++rep)
@@ -265,10 +277,19 @@ struct CgRun {
         return H3D_OK;
     }
 
-    // COLOUR27: keep the stored coefficients only if the chosen implementation uses them
+    // Keep the stored coefficients only if the chosen implementation uses them
     // (a cached choice of them without room for them falls back to the grid's tile shape).
     void settle_coefs()
     {
+        if (order == H3D_ORDER_BLOCK8 && coef && shape >= 0) {
+            int32_t bd[3];
+            int r = 1;
+            block8_cfg_dims(shape, bd, &r);
+            if (bd[0] != 12 || bd[1] != 12 || bd[2] != 12) {  // only the 12^3 kernels read them
+                coefs.release();
+                coef = nullptr;
+            }
+        }
         if (order != H3D_ORDER_COLOUR27) return;
         if (shape == num_tile_shapes() && !coef) shape = pick_tile_shape(op.nx, op.ny, op.nz);
         if (shape != num_tile_shapes() && coef) {
@@ -278,7 +299,11 @@ struct CgRun {
     }
 
     // Stored coefficients for the sweep launches (null: the chosen kernel does not use them).
-    const cplx<T> *cf() const { return (order == H3D_ORDER_COLOUR27 && shape == num_tile_shapes()) ? coef : nullptr; }
+    const cplx<T> *cf() const
+    {
+        if (order == H3D_ORDER_BLOCK8) return coef;
+        return (order == H3D_ORDER_COLOUR27 && shape == num_tile_shapes()) ? coef : nullptr;
+    }
 
     // b~ = DSWP(0, b) into y, then x = 0, r = p = y.
     int setup(const cplx<T> *b, const double *bnorm2_orig, double zero_tol2, cudaStream_t st)

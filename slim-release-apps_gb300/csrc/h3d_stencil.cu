@@ -68,7 +68,7 @@ static int sweep_dispatch(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrh
     } else if (order == H3D_ORDER_BLOCK) {
         rc = sweep_block(op, x, b, nrhs, w, block, active, ADJ, st, rinv, shape);
     } else if (order == H3D_ORDER_BLOCK8) {
-        rc = sweep_block8(op, x, b, nrhs, w, block, active, ADJ, st, rinv, shape);
+        rc = sweep_block8(op, x, b, nrhs, w, block, active, ADJ, st, rinv, shape, coef);
     } else {
         set_error("unknown sweep order %d", order);
         return H3D_ERR_BAD_ARG;

@@ -108,7 +108,9 @@ def test_reordered_sweeps_match_oracle(cuda, golden_small, order, blk, mode):
     assert _rel(y32.cpu().numpy().T.astype(np.complex128), ref) <= 5e-5
 
 
-@pytest.mark.parametrize("order,blk", [(3, (12, 12, 12)), (3, (24, 12, 12)), (1, None), (1, (-1, 0, 0))])
+# BLOCK8 12^3 on stored coefficients (12, 12, 12) and forming them itself (-1, 0, 0)
+@pytest.mark.parametrize("order,blk", [(3, (12, 12, 12)), (3, (-1, 0, 0)), (3, (24, 12, 12)), (1, None),
+                                       (1, (-1, 0, 0))])
 @pytest.mark.parametrize("mode,wnc", [(1, False), (2, False), (1, True), (2, True)])
 def test_block8_and_colour27_sweeps_match_oracle(cuda, order, blk, mode, wnc):
     """BLOCK8 (parity classes of blocks) on a grid of several blocks per axis and COLOUR27
@@ -126,7 +128,8 @@ def test_block8_and_colour27_sweeps_match_oracle(cuda, order, blk, mode, wnc):
         wn = wn * (1.0 + 0.05j * rng.random(N))
     X = rng.standard_normal((N, 3)) + 1j * rng.standard_normal((N, 3))
     B = rng.standard_normal((N, 3)) + 1j * rng.standard_normal((N, 3))
-    ref = O.sweep(g, wn, 1.5, X, B, adj=(mode == 2), order=order, blk=blk if order == 3 else None, nthreads=2)
+    oblk = None if order != 3 else ((12, 12, 12) if blk[0] == -1 else blk)
+    ref = O.sweep(g, wn, 1.5, X, B, adj=(mode == 2), order=order, blk=oblk, nthreads=2)
     grid = (n, h, npml)
     y = ops.kacz_sweep(grid, _t(wn, cuda), 1.5, _t(X.T, cuda, torch.complex128), _t(B.T, cuda, torch.complex128),
                        mode, order=order, block=blk)
