@@ -52,7 +52,7 @@ REF_ITERS_CONFIG1 = 1481
 
 
 # Row order of the timed solves (the solver's tuner then picks the kernel configuration).
-DEFAULT_ORDER = "colour27"
+DEFAULT_ORDER = "block8"
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of the
 # complex64 config-1 solve (python -m h3d.profile --kernel cgmn --config 1 --dtype c64,
