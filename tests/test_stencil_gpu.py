@@ -140,6 +140,32 @@ def test_block8_and_colour27_sweeps_match_oracle(cuda, order, blk, mode, wnc):
     assert _rel(y32.cpu().numpy().T.astype(np.complex128), ref) <= 5e-5
 
 
+@pytest.mark.parametrize("blk", [(12, 12, 12), (-1, 0, 0)])
+@pytest.mark.parametrize("nrhs", [1, 5])
+@pytest.mark.parametrize("mode", [1, 2])
+def test_block8_rhs_groups_match_oracle(cuda, blk, nrhs, mode):
+    """BLOCK8 12^3 kernels by right-hand-side group: one right-hand side runs four lanes per
+    row, five run groups of four (one lane per row, the second group partly filled)."""
+    import torch
+    from h3d import ops
+
+    n, h, npml = (26, 25, 27), (20.0, 20.0, 20.0), (4, 4, 4, 4, 4, 4)
+    rng = np.random.default_rng(41 + nrhs)
+    N = int(np.prod(n))
+    g = O.make_grid(n, h, npml)
+    wn = (2 * np.pi * 5.0) ** 2 / (1500.0 + 1500.0 * rng.random(N)) ** 2
+    X = rng.standard_normal((N, nrhs)) + 1j * rng.standard_normal((N, nrhs))
+    B = rng.standard_normal((N, nrhs)) + 1j * rng.standard_normal((N, nrhs))
+    ref = O.sweep(g, wn, 1.5, X, B, adj=(mode == 2), order=O.ORDER_BLOCK8, blk=(12, 12, 12), nthreads=2)
+    grid = (n, h, npml)
+    y = ops.kacz_sweep(grid, _t(wn, cuda), 1.5, _t(X.T, cuda, torch.complex128), _t(B.T, cuda, torch.complex128),
+                       mode, order=3, block=blk)
+    assert _rel(y.cpu().numpy().T, ref) <= 1e-12
+    y32 = ops.kacz_sweep(grid, _t(wn.astype(np.float32), cuda), 1.5, _t(X.T, cuda, torch.complex64),
+                         _t(B.T, cuda, torch.complex64), mode, order=3, block=blk)
+    assert _rel(y32.cpu().numpy().T.astype(np.complex128), ref) <= 5e-5
+
+
 def test_config0_matvec_golden(cuda):
     """61^3, PML 10: the forward and adjoint matvecs of a seeded complex128 vector,
     against the reference's own output (sampled entries, norm and a probe product)."""
