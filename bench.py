@@ -249,7 +249,7 @@ def run_gpu_arm(args, world, rank):
     wn = torch.as_tensor(m.wavenumber(), device=dev)
     b = torch.as_tensor(m.point_source(), device=dev)
     opts = solver.make_opts(tol=1e-6, precision="mixed", order=args.order, inner_tol=args.inner_tol,
-                            check_every=args.check_every)
+                            check_every=args.check_every, block=args.block)
 
     def step():
         return solver.solve(grid, wn, b, opts=opts)
@@ -354,6 +354,8 @@ def main():
     ap.add_argument("--impl", default="h3d", choices=["h3d", "reference"])
     ap.add_argument("--inner-tol", type=float, default=1e-4)
     ap.add_argument("--order", default=DEFAULT_ORDER, choices=["colour27", "block8", "block", "lex"])
+    ap.add_argument("--block", type=int, nargs=3, default=None,
+                    help="fixed block size for BLOCK/BLOCK8 (skips the solver's measured tuning)")
     ap.add_argument("--check-every", type=int, default=25)
     ap.add_argument("--cpu-sample-iters", type=int, default=4)
     ap.add_argument("--ref-iters", type=int, default=None)

@@ -59,15 +59,13 @@ __global__ void __launch_bounds__(128) coef8_store_kernel(Op<T> op, cplx<T> *coe
     }
 }
 
-// S: lanes per row (1, or 4 with block_row_split).
-template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ, int R, int S>
-__global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R * S) sweep_block8_kernel(
+template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ, int R>
+__global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_block8_kernel(
     Op<T> op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active, const T *rinv,
     const cplx<T> *coef, int NI, int NJ, int NIp, int NJp, int par, int backward)
 {
     static_assert(BX % 3 == 0 && BY % 3 == 0 && BZ % 3 == 0, "block sides must be multiples of 3");
-    static_assert(S == 1 || S == 4, "one or four lanes per row");
-    constexpr int U = BX / 3, V = BY / 3, W = BZ / 3, NR = U * V * W, NT = NR * R * S;
+    constexpr int U = BX / 3, V = BY / 3, W = BZ / 3, NR = U * V * W, NT = NR * R;
     constexpr int SLAB = 27 * NR;
     using G = BlockGeom<BX, BY, BZ>;
     constexpr int PX = G::PX, PY = G::PY, NB = G::NB;
@@ -119,8 +117,7 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R * S) sweep_
     // then v: a half-warp spans (u, w), whose box offsets 3u + 3 PX PY w hit 16 distinct
     // 8-byte bank pairs for the 14-point box pitch (no shared-memory bank conflicts).
     const int tid = threadIdx.x;
-    const int sub = tid % S, slot = tid / S;
-    const int r = slot / NR, row = slot % NR;
+    const int r = tid / NR, row = tid % NR;
     const int u = row % U, ww = (row / U) % W, v = row / (U * W);
     const bool mine = (act >> r) & 1u;
     cplx<T> *bx = sx + (size_t)r * NB;
@@ -153,23 +150,12 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R * S) sweep_
         }
         const int a = q % 3, bq = (q / 3) % 3, cq = q / 9;
         const int i = bi0 + a + 3 * u, j = bj0 + bq + 3 * v, k = bk0 + cq + 3 * ww;
-        const bool valid = mine && i < op.nx && j < op.ny && k < op.nz;
-        const int lc = (1 + a + 3 * u) + PX * ((1 + bq + 3 * v) + PY * (1 + cq + 3 * ww));
-        if constexpr (S == 1) {
-            if (valid) {
-                if (stored)
-                    block_row_stored<T, PX, PY>(op, bx, sc + (qq & 1) * SLAB, NR, row, bv, inv, w, i, j, k, lc);
-                else
-                    block_row<T, ADJ, WNC, PX, PY>(op, bx, swr, swi, bv, inv, w, i, j, k, lc);
-            }
-        } else {
-            const cplx<T> *scq = stored ? sc + (qq & 1) * SLAB : nullptr;
-            switch (sub) {  // every lane takes part (shuffles inside)
-            case 0: block_row_split<T, ADJ, WNC, PX, PY, 0>(op, bx, swr, swi, scq, NR, row, valid, bv, inv, w, i, j, k, lc); break;
-            case 1: block_row_split<T, ADJ, WNC, PX, PY, 1>(op, bx, swr, swi, scq, NR, row, valid, bv, inv, w, i, j, k, lc); break;
-            case 2: block_row_split<T, ADJ, WNC, PX, PY, 2>(op, bx, swr, swi, scq, NR, row, valid, bv, inv, w, i, j, k, lc); break;
-            default: block_row_split<T, ADJ, WNC, PX, PY, 3>(op, bx, swr, swi, scq, NR, row, valid, bv, inv, w, i, j, k, lc); break;
-            }
+        if (mine && i < op.nx && j < op.ny && k < op.nz) {
+            const int lc = (1 + a + 3 * u) + PX * ((1 + bq + 3 * v) + PY * (1 + cq + 3 * ww));
+            if (stored)
+                block_row_stored<T, PX, PY>(op, bx, sc + (qq & 1) * SLAB, NR, row, bv, inv, w, i, j, k, lc);
+            else
+                block_row<T, ADJ, WNC, PX, PY>(op, bx, swr, swi, bv, inv, w, i, j, k, lc);
         }
         __syncthreads();
     }
@@ -178,10 +164,9 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R * S) sweep_
 
 // Block shapes and right-hand-side group sizes the BLOCK8 path can use.
 struct Block8Cfg {
-    int bx, by, bz, r, s;  // block, right-hand sides per CTA, lanes per row
+    int bx, by, bz, r;
 };
-static const Block8Cfg kBlock8Cfgs[] = {{12, 12, 12, 1, 1}, {12, 12, 12, 2, 1}, {12, 12, 12, 4, 1},
-                                        {24, 12, 12, 1, 1}, {12, 12, 12, 1, 4}, {12, 12, 12, 2, 4}};
+static const Block8Cfg kBlock8Cfgs[] = {{12, 12, 12, 1}, {12, 12, 12, 2}, {12, 12, 12, 4}, {24, 12, 12, 1}};
 constexpr int kNumBlock8Cfgs = sizeof(kBlock8Cfgs) / sizeof(kBlock8Cfgs[0]);
 
 int num_block8_cfgs() { return kNumBlock8Cfgs; }
@@ -202,13 +187,13 @@ void block8_cfg_dims(int c, int32_t *blk, int *r)
     *r = kBlock8Cfgs[c].r;
 }
 
-template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ, int R, int S>
+template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ, int R>
 static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active,
                          const T *rinv, const cplx<T> *coef, bool backward, cudaStream_t st)
 {
     constexpr size_t smem_box = block_smem<T, WNC, BX, BY, BZ, R>();
     constexpr size_t smem_coef = ((smem_box + 15) / 16) * 16 + 2 * sizeof(cplx<T>) * Coef8Layout<BX, BY, BZ>::SLAB;
-    constexpr int NT = (BX / 3) * (BY / 3) * (BZ / 3) * R * S;
+    constexpr int NT = (BX / 3) * (BY / 3) * (BZ / 3) * R;
     if constexpr (smem_box > 232448) {  // 227 KB: the per-CTA shared-memory limit
         set_error("BLOCK8 configuration %dx%dx%d x %d right-hand sides exceeds shared memory", BX, BY, BZ, R);
         return H3D_ERR_BAD_ARG;
@@ -219,7 +204,7 @@ static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs
         static bool attr_set = false;  // per template instance and process
         if (!attr_set) {
             const size_t mx = smem_coef > 232448 ? smem_box : smem_coef;
-            H3D_CUDA_TRY(cudaFuncSetAttribute(sweep_block8_kernel<T, ADJ, WNC, BX, BY, BZ, R, S>,
+            H3D_CUDA_TRY(cudaFuncSetAttribute(sweep_block8_kernel<T, ADJ, WNC, BX, BY, BZ, R>,
                                               cudaFuncAttributeMaxDynamicSharedMemorySize, (int)mx));
             attr_set = true;
         }
@@ -239,7 +224,7 @@ static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs
         const dim3 grd((unsigned)nblk, ngrp);
         for (int pp = 0; pp < 8; ++pp) {
             const int par = backward ? 7 - pp : pp;
-            sweep_block8_kernel<T, ADJ, WNC, BX, BY, BZ, R, S><<<grd, NT, smem, st>>>(
+            sweep_block8_kernel<T, ADJ, WNC, BX, BY, BZ, R><<<grd, NT, smem, st>>>(
                 op, x, b, nrhs, w, active, rinv, coef, NI, NJ, NIp, NJp, par, backward ? 1 : 0);
         }
         H3D_CUDA_TRY(cudaGetLastError());
@@ -253,12 +238,10 @@ static int block8_pass_cfg(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nr
 {
     // the stored layout is the 12x12x12 one: the 24x12x12 configuration forms coefficients itself
     switch (cfg) {
-    case 1: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 2, 1>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
-    case 2: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 4, 1>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
-    case 3: return block8_pass_t<T, ADJ, WNC, 24, 12, 12, 1, 1>(op, x, b, nrhs, w, active, rinv, nullptr, backward, st);
-    case 4: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 1, 4>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
-    case 5: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 2, 4>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
-    default: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 1, 1>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
+    case 1: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 2>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
+    case 2: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 4>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
+    case 3: return block8_pass_t<T, ADJ, WNC, 24, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, nullptr, backward, st);
+    default: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
     }
 }
 
@@ -294,10 +277,7 @@ static int cfg8_for_block(const int32_t *blk, int nrhs)
     for (int c = 0; c < kNumBlock8Cfgs; ++c) {
         const Block8Cfg &k = kBlock8Cfgs[c];
         if (k.bx != blk[0] || k.by != blk[1] || k.bz != blk[2]) continue;
-        // the largest group the right-hand sides fill, then the most lanes per row
-        if (best < 0 || (k.r <= nrhs && (k.r > kBlock8Cfgs[best].r ||
-                                          (k.r == kBlock8Cfgs[best].r && k.s > kBlock8Cfgs[best].s))))
-            best = c;
+        if (best < 0 || (k.r <= nrhs && k.r > kBlock8Cfgs[best].r)) best = c;
     }
     return best;
 }

@@ -189,77 +189,4 @@ __device__ __forceinline__ void block_row_stored(const Op<T> &op, cplx<T> *bx, c
 #undef H3D_SS
 }
 
-// One row projected by four lanes of a warp (lanes 4s .. 4s+3, SUB = lane % 4): lane SUB
-// owns the offsets t = SUB (mod 4), 7 or 6 of the 27.  Each lane forms its coefficients
-// (stored: from the staged slab sc; interior row: K_t - WM_t wn; else the PML expressions),
-// gathers its part of a.x, the four parts are summed with two butterfly shuffles, and each
-// lane scatters its own offsets.  Every lane of the warp must call it (valid = false for
-// lanes without a row) because of the shuffles.  Four times the warps of one lane per row,
-// each with about a quarter of the dependent instruction chain: the colour steps of a block
-// are latency-bound, and this is how they get more warps per scheduler.
-template <typename T, bool ADJ, bool WNC, int PX, int PY, int SUB>
-__device__ __forceinline__ void block_row_split(const Op<T> &op, cplx<T> *bx, const T *swr, const T *swi,
-                                                const cplx<T> *sc, int NR, int row, bool valid, cplx<T> bv,
-                                                T inv, T w, int i, int j, int k, int lc)
-{
-    cplx<T> c[27];
-    uint32_t m = 0x7ffffffu;
-    cplx<T> acc = mk<T>(T(0), T(0));
-    if (valid) {
-        auto wnf = [&](int dx, int dy, int dz) {
-            const int qd = lc + dx + PX * (dy + PY * dz);
-            return mk<T>(swr[qd], WNC ? swi[qd] : T(0));
-        };
-        auto wnr = [&](int dx, int dy, int dz) { return swr[lc + dx + PX * (dy + PY * dz)]; };
-        if (sc) {
-            const bool edge = i == 0 || j == 0 || k == 0 || i == op.nx - 1 || j == op.ny - 1 || k == op.nz - 1;
-            if (edge) m = inside_mask(i, j, k, op.nx, op.ny, op.nz);
-#define H3D_LS(t, dx, dy, dz) if constexpr ((t) % 4 == SUB) c[t] = sc[(t) * NR + row];
-            H3D_FOR_27(H3D_LS)
-#undef H3D_LS
-        } else {
-            const int *ilo = ADJ ? op.int_lo_a : op.int_lo_f, *ihi = ADJ ? op.int_hi_a : op.int_hi_f;
-            const bool interior =
-                !WNC && i >= ilo[0] && i < ihi[0] && j >= ilo[1] && j < ihi[1] && k >= ilo[2] && k < ihi[2];
-            if (interior) {
-#define H3D_LI(t, dx, dy, dz) if constexpr ((t) % 4 == SUB) c[t] = mk<T>(coef_int<t, dx, dy, dz, T, ADJ>(op, wnr), T(0));
-                H3D_FOR_27(H3D_LI)
-#undef H3D_LI
-            } else {
-                const RowPml<T> pml = load_row_pml<T, ADJ>(op, i, j, k);
-                m = inside_mask(i, j, k, op.nx, op.ny, op.nz);
-#define H3D_LP(t, dx, dy, dz) \
-    if constexpr ((t) % 4 == SUB) c[t] = coef_at<t, dx, dy, dz, T, ADJ, false, WNC>(op, pml, ADJ ? 0x7ffffffu : m, wnf);
-                H3D_FOR_27(H3D_LP)
-#undef H3D_LP
-            }
-        }
-#define H3D_LG(t, dx, dy, dz)                                                                  \
-    if constexpr ((t) % 4 == SUB) {                                                            \
-        const cplx<T> xv = bx[lc + dx + PX * (dy + PY * dz)];                                  \
-        acc.re += c[t].re * xv.re - c[t].im * xv.im;                                           \
-        acc.im += c[t].re * xv.im + c[t].im * xv.re;                                           \
-    }
-        H3D_FOR_27(H3D_LG)
-#undef H3D_LG
-    }
-    acc.re += __shfl_xor_sync(0xffffffffu, acc.re, 1);
-    acc.im += __shfl_xor_sync(0xffffffffu, acc.im, 1);
-    acc.re += __shfl_xor_sync(0xffffffffu, acc.re, 2);
-    acc.im += __shfl_xor_sync(0xffffffffu, acc.im, 2);
-    if (!valid) return;
-    const cplx<T> d = (w * inv) * (bv - acc);
-#define H3D_LSC(t, dx, dy, dz)                                                                 \
-    if constexpr ((t) % 4 == SUB) {                                                            \
-        if (m & (1u << t)) {                                                                   \
-            cplx<T> &o = bx[lc + dx + PX * (dy + PY * dz)];                                    \
-            o.re += d.re * c[t].re + d.im * c[t].im;                                           \
-            o.im += d.im * c[t].re - d.re * c[t].im;                                           \
-        }                                                                                      \
-    }
-    H3D_FOR_27(H3D_LSC)
-#undef H3D_LSC
-}
-
 }  // namespace h3d
-

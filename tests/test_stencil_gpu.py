@@ -144,8 +144,8 @@ def test_block8_and_colour27_sweeps_match_oracle(cuda, order, blk, mode, wnc):
 @pytest.mark.parametrize("nrhs", [1, 5])
 @pytest.mark.parametrize("mode", [1, 2])
 def test_block8_rhs_groups_match_oracle(cuda, blk, nrhs, mode):
-    """BLOCK8 12^3 kernels by right-hand-side group: one right-hand side runs four lanes per
-    row, five run groups of four (one lane per row, the second group partly filled)."""
+    """BLOCK8 12^3 kernels by right-hand-side group: one right-hand side per block, and five
+    in groups of four (the second group partly filled)."""
     import torch
     from h3d import ops
 
