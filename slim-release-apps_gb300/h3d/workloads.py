@@ -25,7 +25,7 @@ def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def config2(order="block", precision="mixed", freqs=None, nsrc=None, tol=1e-6, inner_tol=1e-4):
+def config2(order="block8", precision="mixed", freqs=None, nsrc=None, tol=1e-6, inner_tol=1e-4):
     """64 surface sources x {3,4,5,6} Hz on the config-1 model: one problem per frequency,
     the sources of a frequency as right-hand sides of one batched solve."""
     m = models.config2()
@@ -57,7 +57,7 @@ def config2(order="block", precision="mixed", freqs=None, nsrc=None, tol=1e-6, i
             "nsrc": len(srcs)}
 
 
-def config3_problem(precision="mixed", order="block", nsrc=None, freqs=None):
+def config3_problem(precision="mixed", order="block8", nsrc=None, freqs=None):
     m = models.config3()
     meta = m.meta
     src = meta["src_xyz"] if nsrc is None else meta["src_xyz"][:nsrc]
@@ -70,7 +70,7 @@ def config3_problem(precision="mixed", order="block", nsrc=None, freqs=None):
     return prob, m_true, m0
 
 
-def config3(precision="mixed", order="block", nsrc=None, freqs=None):
+def config3(precision="mixed", order="block8", nsrc=None, freqs=None):
     """FWI gradient w.r.t. squared slowness: 32 jittered surface sources, 400 receivers,
     3 / 4.5 / 6 Hz on 161 x 161 x 81 (15-point PML); observed data modelled on the true
     model, gradient at the background model through the autograd function."""
@@ -133,9 +133,9 @@ def main(argv=None):
     a = ap.parse_args(argv)
     t0 = time.time()
     if a.config == 2:
-        out = config2(order=a.order or "block", precision=a.precision, freqs=a.freqs, nsrc=a.nsrc)
+        out = config2(order=a.order or "block8", precision=a.precision, freqs=a.freqs, nsrc=a.nsrc)
     elif a.config == 3:
-        out = config3(precision=a.precision, order=a.order or "block", nsrc=a.nsrc, freqs=a.freqs)
+        out = config3(precision=a.precision, order=a.order or "block8", nsrc=a.nsrc, freqs=a.freqs)
     else:
         out = config4(precision=a.precision, order=a.order or "colour27", nprob=a.nprob)
     out["wall_s"] = time.time() - t0
