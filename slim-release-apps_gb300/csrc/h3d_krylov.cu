@@ -143,8 +143,17 @@ __global__ void k_ap_dot(const cplx<T> *__restrict__ p, cplx<T> *__restrict__ y,
             pv[u] = ps[q + u * stride];
             yv[u] = ys[q + u * stride];
         }
+        // the step's kVecUnroll products summed in T, then added to the FP64 accumulators
+        T sre = T(0), sim = T(0);
 #pragma unroll
-        for (int u = 0; u < kVecUnroll; ++u) body(pv[u], yv[u], q + u * stride);
+        for (int u = 0; u < kVecUnroll; ++u) {
+            const cplx<T> ap = pv[u] - yv[u];
+            ys[q + u * stride] = ap;
+            sre = fma(pv[u].re, ap.re, fma(pv[u].im, ap.im, sre));
+            sim = fma(pv[u].re, ap.im, fma(-pv[u].im, ap.re, sim));
+        }
+        are += (double)sre;
+        aim += (double)sim;
     }
     for (; q < N; q += stride) body(ps[q], ys[q], q);
     const double2 t = block_sum2(are, aim);
@@ -215,8 +224,15 @@ __global__ void k_update_xr(cplx<T> *__restrict__ x, cplx<T> *__restrict__ r,
             xv[u] = xs[q + u * stride];
             rv[u] = rs[q + u * stride];
         }
+        T sr = T(0);  // the step's squared norms summed in T, then added in FP64
 #pragma unroll
-        for (int u = 0; u < kVecUnroll; ++u) body(pv[u], av[u], xv[u], rv[u], q + u * stride);
+        for (int u = 0; u < kVecUnroll; ++u) {
+            const cplx<T> xn = xv[u] + pv[u] * a, rn = rv[u] - av[u] * a;
+            xs[q + u * stride] = xn;
+            rs[q + u * stride] = rn;
+            sr = fma(rn.re, rn.re, fma(rn.im, rn.im, sr));
+        }
+        acc += (double)sr;
     }
     for (; q < N; q += stride) body(ps[q], as[q], xs[q], rs[q], q);
     const double2 t = block_sum2(acc, 0.0);
