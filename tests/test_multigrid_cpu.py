@@ -1,0 +1,58 @@
+"""The oracle's restatement of FGMRES + ML_GMRES (oracle/slim_ml.py) on CPU.
+
+* opLInterp1D's self-test (opLInterp1D.m test()): cubic Lagrange weights reproduce x^3
+  exactly on points inside the node range, and the operator's adjoint passes the dot test;
+* LinInterp1D reproduces linear functions, and the multigrid restriction is (1/8) times the
+  adjoint of the prolongation (construct_multigrid.m:45-51);
+* FGMRES (FGMRES.m) solves a small dense system, with and without a preconditioner;
+* FGMRES preconditioned by the three-level ML_GMRES V-cycle solves a small Helmholtz problem
+  to the requested true residual.
+"""
+import numpy as np
+
+from oracle import slim_ml as ML
+
+
+def test_interpolation_operators():
+    rng = np.random.default_rng(0)
+    x1 = np.linspace(0, 1, 13)
+    x2 = np.linspace(0, 1, 7)
+    A = ML.cubic_interp_1d(x1, x2)
+    assert np.max(np.abs(A @ x1 ** 3 - x2 ** 3)) <= 1e-12
+    f1, f2 = rng.standard_normal(13), rng.standard_normal(7)
+    assert abs(1 - (A @ f1) @ f2 / (f1 @ (A.T @ f2))) <= 1e-10
+    L = ML.lin_interp_1d(np.linspace(0, 1, 7), np.linspace(0, 1, 13))
+    assert np.max(np.abs(L @ (3 * np.linspace(0, 1, 7) + 1) - (3 * np.linspace(0, 1, 13) + 1))) <= 1e-12
+    f2c, c2f, nsub = ML.fine2coarse((9, 8, 7), kind="linear", n_sub=(5, 4, 4))
+    x = rng.standard_normal(9 * 8 * 7)
+    y = rng.standard_normal(5 * 4 * 4)
+    assert abs((c2f * y) @ x - y @ (f2c * x)) <= 1e-10 * np.linalg.norm(x) * np.linalg.norm(y)
+
+
+def test_fgmres_dense():
+    rng = np.random.default_rng(1)
+    n = 30
+    M = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n) + 3 * np.eye(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    ref = np.linalg.solve(M, b)
+    x, res, hst = ML.fgmres(lambda v: M @ v, b, None, tol=1e-10, maxit=50, maxinnerit=5)
+    assert np.linalg.norm(x - ref) <= 1e-8 * np.linalg.norm(ref)
+    D = np.diag(1.0 / np.diag(M))
+    x2, _, hst2 = ML.fgmres(lambda v: M @ v, b, None, tol=1e-10, maxit=50, maxinnerit=5, precond=lambda v: D @ v)
+    assert np.linalg.norm(x2 - ref) <= 1e-8 * np.linalg.norm(ref)
+
+
+def test_ml_gmres_solves_small_helmholtz():
+    rng = np.random.default_rng(0)
+    n, h = (17, 15, 13), 25.0
+    z = np.arange(n[2]) * h
+    v = np.broadcast_to(1500 + 1000 * z / z[-1], n).copy() * (1 + 0.05 * rng.standard_normal(n))
+    levels, R, P = ML.build_levels(v, (h, h, h), 6, 4.0, "m/s")
+    assert [l.nt for l in levels] == [(29, 27, 25), (15, 14, 13), (9, 8, 8)]
+    b = np.zeros(levels[0].N, complex)
+    nx, ny, _ = levels[0].nt
+    b[nx // 2 + nx * (ny // 2) + nx * ny * 9] = 1.0
+    x, res, hst = ML.ml_gmres_solve(levels, R, P, b, tol=1e-6)
+    r = b - levels[0].A(x)
+    assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-6
+    assert len(hst) - 1 <= 25
