@@ -29,6 +29,9 @@
  *   h3d_src_inject,    sinc-Kaiser source injection Ps and receiver sampling Pr
  *   h3d_rec_sample,    (opInterp.m:34-58, opSincInterp.m:26-70, DataGrid.m:22-44)
  *   h3d_rec_spread
+ *   h3d_axis_apply     grid transfers of the ML_GMRES multigrid preconditioner
+ *                      (construct_multigrid.m:45-51, fine2coarse.m:40-55: Kronecker
+ *                       products of 1D interpolation operators, one axis per call)
  *
  * Every call is asynchronous on the given CUDA stream (NULL = legacy default
  * stream) unless documented otherwise; all pointers are device pointers unless
@@ -245,6 +248,14 @@ int h3d_rec_sample(const h3d_grid *g, const int32_t *base, const double *w, int 
 /* b_s = scale * Pr^T d_s   (adjoint source; b is overwritten). */
 int h3d_rec_spread(const h3d_grid *g, const int32_t *base, const double *w, int nrec,
                    const void *d, int nrhs, double scale, void *b, void *stream);
+
+/* ---- multigrid grid transfer -------------------------------------------------------- */
+/* y = A x along one axis of a complex 3D field: A is n_out x dims_in[axis] in CSR form
+ * (rowptr[n_out + 1], col, val in double; device pointers; every col < dims_in[axis]),
+ * x has dims_in (x fastest) and y the same dims with dims[axis] = n_out, nrhs fields each
+ * (dtype C128 or C64; the sums are formed in double). */
+int h3d_axis_apply(const int32_t *rowptr, const int32_t *col, const double *val, int n_out, int axis,
+                   const int32_t dims_in[3], const void *x, void *y, int nrhs, int dtype, void *stream);
 
 #ifdef __cplusplus
 }

@@ -97,6 +97,8 @@ _SIGS = {
     "h3d_rec_sample": (C.c_int, [C.POINTER(Grid), vp, vp, C.c_int, vp, C.c_int, vp, vp]),
     "h3d_rec_spread": (C.c_int, [C.POINTER(Grid), vp, vp, C.c_int, vp, C.c_int, C.c_double, vp,
                                  vp]),
+    "h3d_axis_apply": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.POINTER(C.c_int32), vp, vp, C.c_int,
+                                 C.c_int, vp]),
 }
 
 EXPORTED = sorted(_SIGS)
