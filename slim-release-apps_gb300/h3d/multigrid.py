@@ -79,7 +79,7 @@ def cubic_weights(x1, x2):
         nodes = (b - 1, b, c, c + 1)
         for p in nodes:
             others = [q for q in nodes if q != p]
-            A[k, p] += np.prod([(X - x1[q]) for q in others]) / np.prod([(x1[p] - x1[q]) for q in others])
+            A[k, p] += np.prod([X - x1[q] for q in others]) / np.prod([x1[p] - x1[q] for q in others])
     return A
 
 
@@ -87,7 +87,9 @@ def _coarsen_model(v, n_sub):
     """Physical model on ceil(n/2) points per axis by separable cubic interpolation."""
     g = lambda m: np.linspace(0.0, 1.0, int(m))
     Ax, Ay, Az = (cubic_weights(g(v.shape[a]), g(n_sub[a])) for a in range(3))
-    return np.einsum("ai,bj,ck,ijk->abc", Ax, Ay, Az, v)
+    t = np.tensordot(Ax, v, axes=(1, 0))                        # (a, j, k)
+    t = np.tensordot(Ay, t, axes=(1, 1)).transpose(1, 0, 2)     # (a, b, k)
+    return np.tensordot(t, Az, axes=(2, 1))                     # (a, b, c)
 
 
 def _extend(v, npml):
@@ -159,10 +161,12 @@ class Level:
         self.nt = tuple(int(n + 2 * self.npml) for n in self.v_phys.shape)
         wn = _wavenumber(_extend(self.v_phys, self.npml), freq, unit)
         self.wn = torch.as_tensor(wn.reshape(-1, order="F").copy(), device=dev)
+        self.wn32 = self.wn.float()
         self.grid = L.make_grid(self.nt, self.dt, (self.npml,) * 6)
 
     def A(self, x: torch.Tensor, mode: int = 1) -> torch.Tensor:
-        return ops.mvp(self.grid, self.wn, x, mode)
+        """H x (mode 1) or H^H x in the precision of x (complex128 or complex64)."""
+        return ops.mvp(self.grid, self.wn if x.dtype == torch.complex128 else self.wn32, x, mode)
 
 
 def build_levels(v_phys, dt, npml, freq, unit="m/s", nlevels=3, device=None):
@@ -271,11 +275,22 @@ class MLGMRES:
         return self.vcycle(0, b, mode)
 
 
-def solve(levels, R, P, b: torch.Tensor, tol=1e-6, maxit=10000, maxinnerit=5, mode=1):
+def solve(levels, R, P, b: torch.Tensor, tol=1e-6, maxit=10000, maxinnerit=5, mode=1, precision="fp64"):
     """u = H \\ b by FGMRES + ML_GMRES, as linearsolve with SOLVE_FGMRES and PREC_MLGMRES.
+
+    precision "fp64": everything in complex128 (the reference's arithmetic).  "mixed": the
+    outer FGMRES (its matvecs, Krylov basis and stopping test) stays complex128 and the
+    V-cycle runs in complex64 -- FGMRES allows a preconditioner that changes between
+    applications, so the inexact single-precision cycle only affects the iteration count.
     Returns (u, info) with the outer iteration count and the quasi-residual history."""
     T = MLGMRES(levels, R, P)
     A0 = lambda v: levels[0].A(v, mode)
+    if precision == "fp64":
+        pre = lambda v: T(v, mode)
+    elif precision == "mixed":
+        pre = lambda v: T(v.to(torch.complex64), mode).to(torch.complex128)
+    else:
+        raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
     u, res, hst = fgmres(A0, b.to(torch.complex128), None, tol=tol, maxit=maxit, maxinnerit=maxinnerit,
-                         precond=lambda v: T(v, mode))
+                         precond=pre)
     return u, {"iters": len(hst) - 1, "hst": hst, "res": res}

@@ -62,3 +62,21 @@ def test_fgmres_ml_gmres_matches_oracle(cuda):
     assert np.linalg.norm(u - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
     r = b - lv_ref[0].A(u)
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-6
+
+
+def test_mixed_precision_cycle_converges(cuda):
+    """complex64 V-cycle under the complex128 FGMRES: the same true residual, at most a
+    few more outer iterations than the FP64 solve."""
+    import torch
+    from h3d import multigrid as MG
+
+    v, dt, npml, f = _model(seed=3)
+    lv, R, P = MG.build_levels(v, dt, npml, f, "m/s", device=cuda)
+    b = torch.zeros(int(np.prod(lv[0].nt)), dtype=torch.complex128, device=cuda)
+    nx, ny, _ = lv[0].nt
+    b[nx // 2 + nx * (ny // 2) + nx * ny * 9] = 1.0
+    u64, i64 = MG.solve(lv, R, P, b, tol=1e-6)
+    u32, i32 = MG.solve(lv, R, P, b, tol=1e-6, precision="mixed")
+    for u in (u64, u32):
+        assert float((b - lv[0].A(u)).norm() / b.norm()) <= 1e-6
+    assert i32["iters"] <= i64["iters"] + 5
