@@ -202,6 +202,14 @@ static int make_op(const h3d_grid *g, const T *wn, const T *wni, Op<T> *op)
     o.kint[5] = (T)(-2 * (double)o.xz + 2 * (double)o.w3a2);
     o.kint[6] = (T)(-2 * (double)o.yz + 2 * (double)o.w3a2);
     o.kint[7] = (T)(-3 * (double)o.w3a2);
+    o.kxy[0] = (T)((double)o.pml_x + 2 * (double)o.xy);
+    o.kxy[1] = (T)((double)o.pml_y + 2 * (double)o.xy);
+    o.kxy[2] = (T)(-2 * (double)o.xy);
+    o.kxy[3] = (T)(2 * ((double)o.wn_x + (double)o.wn_y));
+    o.kxy[4] = (T)(-(double)o.xz + 2 * (double)o.w3a2);
+    o.kxy[5] = (T)(-(double)o.yz + 2 * (double)o.w3a2);
+    o.kxy[6] = (T)(-2 * (double)o.w3a2);
+    o.kxy[7] = (T)(2 * ((double)o.xz + (double)o.yz));
     // Row ranges whose PML values are exactly 1 (and whose neighbours are all inside the
     // grid), from the same FP64 tables the kernels use.
     {

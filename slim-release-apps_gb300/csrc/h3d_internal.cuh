@@ -73,6 +73,10 @@ struct Op {
     // Interior (all xi = 1): PML part of the coefficient per offset class
     // [centre, face x, face y, face z, edge xy, edge xz, edge yz, corner].
     T kint[8];
+    // Rows whose x and y PML values are all 1 but whose z values are not: the x/y brackets
+    // fold into one real-weighted sum.  [in-plane: fx, fy, corners, centre; plane above or
+    // below: fx, fy, corners, centre].
+    T kxy[8];
     // Row index ranges [lo, hi) per axis whose PML values are all 1, for the forward
     // rows (xi_lo(i) = xi_hi(i) = 1) and the adjoint rows (xi_hi(i-1) = xi_lo(i+1) = 1
     // and xi_lo(i) + xi_hi(i) = 2).

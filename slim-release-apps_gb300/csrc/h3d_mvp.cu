@@ -74,6 +74,12 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
 
     RowPml<T> pml{};
     if (valid && !DERIV) pml = load_row_pml<T, ADJ>(op, i, j, 0);
+    // Columns whose x and y PML values are all 1 across the CTA (uniform): folded brackets;
+    // rows inside the z interior as well: the interior class constants.
+    const int *ilo = ADJ ? op.int_lo_a : op.int_lo_f, *ihi = ADJ ? op.int_hi_a : op.int_hi_f;
+    const bool xyint = !DERIV && !WNC && i0 >= ilo[0] && i0 + kMX <= ihi[0] && j0 >= ilo[1] &&
+                       j0 + kMY <= ihi[1];
+    auto zint = [&](int k) { return k >= ilo[2] && k < ihi[2]; };
     const int l = (threadIdx.x + 1) + kPX * (threadIdx.y + 1);
     // Register queue: brackets of the rows pk-1 (A0), pk (A1) and pk+1 (A2) while plane pk
     // is staged; plane pk completes row pk-1.
@@ -96,9 +102,18 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
         {
             const PlaneSums<T> P = plane_sums<T, ADJ, WNC, kPX>(sx[buf], NEED_WN ? swr[buf] : nullptr,
                                                                 NEED_WN && WNC ? swi[buf] : nullptr, l);
-            acc_plane<2, T, DERIV>(A0, P, op);
-            acc_plane<1, T, DERIV>(A1, P, op);
-            acc_plane<0, T, DERIV>(A2, P, op);
+            if (xyint) {
+                if (zint(pk - 1)) acc_plane_xy<2, T, true>(A0, P, op);
+                else acc_plane_xy<2, T, false>(A0, P, op);
+                if (zint(pk)) acc_plane_xy<1, T, true>(A1, P, op);
+                else acc_plane_xy<1, T, false>(A1, P, op);
+                if (zint(pk + 1)) acc_plane_xy<0, T, true>(A2, P, op);
+                else acc_plane_xy<0, T, false>(A2, P, op);
+            } else {
+                acc_plane<2, T, DERIV>(A0, P, op);
+                acc_plane<1, T, DERIV>(A1, P, op);
+                acc_plane<0, T, DERIV>(A2, P, op);
+            }
         }
         __syncthreads();
         const int k = pk - 1;  // row completed by this plane
@@ -119,7 +134,9 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
             const long long ctr = i + op.sy * j + op.sz * k;
             cplx<T> wc = mk<T>(T(0), T(0));
             if constexpr (ADJ) wc = load_wn<T, WNC>(op, ctr);
-            const cplx<T> v = acc_finish<T, ADJ, DERIV, WNC>(A0, p, wc);
+            const cplx<T> v = !xyint     ? acc_finish<T, ADJ, DERIV, WNC>(A0, p, wc)
+                              : zint(k) ? acc_finish_xy<T, ADJ, true>(A0, p, wc)
+                                        : acc_finish_xy<T, ADJ, false>(A0, p, wc);
             if constexpr (RESID) {
                 const cplx<T> bv = b[(long long)s * op.N + ctr];
                 const cplx<T> r = bv - v;

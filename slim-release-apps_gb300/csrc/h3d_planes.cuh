@@ -144,4 +144,57 @@ __device__ __forceinline__ cplx<T> acc_finish(const RowAcc<T> &a, const RowPml<T
     return y;
 }
 
+// Rows whose x and y PML values are all 1 (A = 1, S = 2): the x/y brackets fold into one
+// real-weighted sum r (kept in a.bsx) with the constants Op::kxy; ZI: the row's z values
+// are 1 as well, and every bracket folds into r with the interior class constants Op::kint.
+// The mass part is accumulated as in acc_plane.
+template <int ROLE, typename T, bool ZI>
+__device__ __forceinline__ void acc_plane_xy(RowAcc<T> &a, const PlaneSums<T> &P, const Op<T> &op)
+{
+    if constexpr (ROLE == 1) {
+        fma_rc(a.mass, op.wn_c, P.wm);
+        fma_rc(a.mass, T(-kWM2), P.wfx + P.wfy);
+        fma_rc(a.mass, T(-kWM3), P.wc4);
+    } else {
+        fma_rc(a.mass, T(-kWM2), P.wm);
+        fma_rc(a.mass, T(-kWM3), P.wfx + P.wfy);
+        fma_rc(a.mass, T(-kWM4), P.wc4);
+    }
+    const cplx<T> fx = P.fxm + P.fxp, fy = P.fym + P.fyp, c4 = P.cxm + P.cxp;
+    cplx<T> &r = a.bsx;
+    if constexpr (ZI) {
+        if constexpr (ROLE == 1) {
+            fma_rc(r, op.kint[1], fx); fma_rc(r, op.kint[2], fy); fma_rc(r, op.kint[4], c4); fma_rc(r, op.kint[0], P.m);
+        } else {
+            fma_rc(r, op.kint[5], fx); fma_rc(r, op.kint[6], fy); fma_rc(r, op.kint[7], c4); fma_rc(r, op.kint[3], P.m);
+        }
+    } else {
+        const T w3 = op.w3a2;
+        if constexpr (ROLE == 1) {
+            fma_rc(r, op.kxy[0], fx); fma_rc(r, op.kxy[1], fy); fma_rc(r, op.kxy[2], c4); fma_rc(r, op.kxy[3], P.m);
+            fma_rc(a.bsz, op.wn_z, P.m); fma_rc(a.bsz, op.xz, fx); fma_rc(a.bsz, op.yz, fy); fma_rc(a.bsz, w3, c4);
+        } else {
+            fma_rc(r, op.kxy[4], fx); fma_rc(r, op.kxy[5], fy); fma_rc(r, op.kxy[6], c4); fma_rc(r, op.kxy[7], P.m);
+            cplx<T> &bz = ROLE == 0 ? a.bzm : a.bzp;
+            fma_rc(bz, op.pml_z, P.m); fma_rc(bz, -op.xz, fx); fma_rc(bz, -op.yz, fy); fma_rc(bz, -w3, c4);
+        }
+    }
+}
+
+// Row value from the folded accumulators (ZI: no z brackets left).
+template <typename T, bool ADJ, bool ZI>
+__device__ __forceinline__ cplx<T> acc_finish_xy(const RowAcc<T> &a, const RowPml<T> &p, cplx<T> wc)
+{
+    cplx<T> y = a.mass;
+    if constexpr (ADJ) y = mk<T>(wc.re * y.re, wc.re * y.im);
+    y = y + a.bsx;
+    if constexpr (!ZI) {
+        auto f = [&](cplx<T> v) { return ADJ ? cconj(v) : v; };
+        cmac(y, f(p.Azm), a.bzm);
+        cmac(y, f(p.Azp), a.bzp);
+        cmac(y, f(p.Sz), a.bsz);
+    }
+    return y;
+}
+
 }  // namespace h3d
