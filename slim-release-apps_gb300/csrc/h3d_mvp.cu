@@ -56,17 +56,34 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
     const bool valid = i < op.nx && j < op.ny;
     const cplx<T> *xs = x + (long long)s * op.N;
 
+    // Staging: the CTA's halo'd plane has kPN points; thread tid copies points tid and
+    // tid + kMX*kMY.  Their in-plane offsets and x/y bounds are fixed for the march.
+    constexpr int kNT = kMX * kMY;
+    constexpr int kSlots = (kPN + kNT - 1) / kNT;
+    long long goff[kSlots];
+    bool gin[kSlots];
+#pragma unroll
+    for (int q = 0; q < kSlots; ++q) {
+        const int e = tid + q * kNT;
+        const int li = e % kPX, lj = e / kPX;
+        const int gi = i0 - 1 + li, gj = j0 - 1 + lj;
+        gin[q] = e < kPN && gi >= 0 && gi < op.nx && gj >= 0 && gj < op.ny;
+        goff[q] = gin[q] ? gi + op.sy * gj : 0;
+    }
     auto stage = [&](int buf, int pk) {
         const bool kin = pk >= 0 && pk < op.nz;
-        for (int e = tid; e < kPN; e += kMX * kMY) {
-            const int li = e % kPX, lj = e / kPX;
-            const int gi = i0 - 1 + li, gj = j0 - 1 + lj;
-            const bool in = kin && gi >= 0 && gi < op.nx && gj >= 0 && gj < op.ny;
-            const long long g = in ? gi + op.sy * gj + op.sz * pk : 0;
-            mv_cp_async<sizeof(cplx<T>)>(&sx[buf][e], xs + g, in);
-            if constexpr (NEED_WN) {
-                mv_cp_async<sizeof(T)>(&swr[buf][e], op.wn + g, in);
-                if constexpr (WNC) mv_cp_async<sizeof(T)>(&swi[buf][e], op.wni + g, in);
+        const long long zo = kin ? op.sz * pk : 0;
+#pragma unroll
+        for (int q = 0; q < kSlots; ++q) {
+            const int e = tid + q * kNT;
+            if (e < kPN) {
+                const bool in = kin && gin[q];
+                const long long g = in ? goff[q] + zo : 0;
+                mv_cp_async<sizeof(cplx<T>)>(&sx[buf][e], xs + g, in);
+                if constexpr (NEED_WN) {
+                    mv_cp_async<sizeof(T)>(&swr[buf][e], op.wn + g, in);
+                    if constexpr (WNC) mv_cp_async<sizeof(T)>(&swi[buf][e], op.wni + g, in);
+                }
             }
         }
         asm volatile("cp.async.commit_group;\n" ::: "memory");
@@ -81,16 +98,12 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
                        j0 + kMY <= ihi[1];
     auto zint = [&](int k) { return k >= ilo[2] && k < ihi[2]; };
     const int l = (threadIdx.x + 1) + kPX * (threadIdx.y + 1);
-    // Register queue: brackets of the rows pk-1 (A0), pk (A1) and pk+1 (A2) while plane pk
-    // is staged; plane pk completes row pk-1.
-    RowAcc<T> A0, A1, A2;
-    acc_zero(A0);
-    acc_zero(A1);
-    acc_zero(A2);
     double rr = 0.0, bb = 0.0;
 
-    stage(0, kb - 1);
-    for (int pk = kb - 1; pk <= ke; ++pk) {
+    // One plane pk: add it to the pending rows pk-1 (lo), pk (mid) and pk+1 (hi), finish
+    // row pk-1 and clear its accumulator, which then serves row pk+2.  The caller rotates
+    // the three accumulators' roles, so no accumulator is ever copied.
+    auto step = [&](int pk, RowAcc<T> &lo, RowAcc<T> &mid, RowAcc<T> &hi) {
         const int buf = (pk - (kb - 1)) & 1;
         if (pk + 1 <= ke) {
             stage(buf ^ 1, pk + 1);
@@ -103,16 +116,16 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
             const PlaneSums<T> P = plane_sums<T, ADJ, WNC, kPX>(sx[buf], NEED_WN ? swr[buf] : nullptr,
                                                                 NEED_WN && WNC ? swi[buf] : nullptr, l);
             if (xyint) {
-                if (zint(pk - 1)) acc_plane_xy<2, T, true>(A0, P, op);
-                else acc_plane_xy<2, T, false>(A0, P, op);
-                if (zint(pk)) acc_plane_xy<1, T, true>(A1, P, op);
-                else acc_plane_xy<1, T, false>(A1, P, op);
-                if (zint(pk + 1)) acc_plane_xy<0, T, true>(A2, P, op);
-                else acc_plane_xy<0, T, false>(A2, P, op);
+                if (zint(pk - 1)) acc_plane_xy<2, T, true>(lo, P, op);
+                else acc_plane_xy<2, T, false>(lo, P, op);
+                if (zint(pk)) acc_plane_xy<1, T, true>(mid, P, op);
+                else acc_plane_xy<1, T, false>(mid, P, op);
+                if (zint(pk + 1)) acc_plane_xy<0, T, true>(hi, P, op);
+                else acc_plane_xy<0, T, false>(hi, P, op);
             } else {
-                acc_plane<2, T, DERIV>(A0, P, op);
-                acc_plane<1, T, DERIV>(A1, P, op);
-                acc_plane<0, T, DERIV>(A2, P, op);
+                acc_plane<2, T, DERIV>(lo, P, op);
+                acc_plane<1, T, DERIV>(mid, P, op);
+                acc_plane<0, T, DERIV>(hi, P, op);
             }
         }
         __syncthreads();
@@ -134,9 +147,9 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
             const long long ctr = i + op.sy * j + op.sz * k;
             cplx<T> wc = mk<T>(T(0), T(0));
             if constexpr (ADJ) wc = load_wn<T, WNC>(op, ctr);
-            const cplx<T> v = !xyint     ? acc_finish<T, ADJ, DERIV, WNC>(A0, p, wc)
-                              : zint(k) ? acc_finish_xy<T, ADJ, true>(A0, p, wc)
-                                        : acc_finish_xy<T, ADJ, false>(A0, p, wc);
+            const cplx<T> v = !xyint     ? acc_finish<T, ADJ, DERIV, WNC>(lo, p, wc)
+                              : zint(k) ? acc_finish_xy<T, ADJ, true>(lo, p, wc)
+                                        : acc_finish_xy<T, ADJ, false>(lo, p, wc);
             if constexpr (RESID) {
                 const cplx<T> bv = b[(long long)s * op.N + ctr];
                 const cplx<T> r = bv - v;
@@ -147,9 +160,18 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
                 y[(long long)s * op.N + ctr] = v;
             }
         }
-        A0 = A1;
-        A1 = A2;
-        acc_zero(A2);
+        acc_zero(lo);
+    };
+
+    RowAcc<T> Q0, Q1, Q2;  // rows pk-1, pk, pk+1 at the top of the loop
+    acc_zero(Q0);
+    acc_zero(Q1);
+    acc_zero(Q2);
+    stage(0, kb - 1);
+    for (int pk = kb - 1; pk <= ke; pk += 3) {
+        step(pk, Q0, Q1, Q2);
+        if (pk + 1 <= ke) step(pk + 1, Q1, Q2, Q0);
+        if (pk + 2 <= ke) step(pk + 2, Q2, Q0, Q1);
     }
     if constexpr (RESID) {
         const double2 t = block_sum2_r(rr, bb);
