@@ -125,6 +125,11 @@ class FWIConfig:
     hbm_budget_bytes: float = 40e9        # keep forward wavefields up to this size
     src_batch: int = 0                    # 0 = all sources of a frequency in one batch
     extra: dict = field(default_factory=dict)
+    # "cgmn": the Kaczmarz-preconditioned CGMN solver (batched over sources);
+    # "mlgmres": FGMRES + ML_GMRES multigrid (h3d.multigrid), one source at a time --
+    # the reference's default for its 3D applications (fwi_exp.m:58-62).  Needs the same
+    # PML width on all six faces.
+    solver: str = "cgmn"
 
 
 class FWIProblem:
@@ -198,10 +203,40 @@ class FWIProblem:
         bs = self.cfg.src_batch or self.nsrc
         return [list(range(s, min(s + bs, self.nsrc))) for s in range(0, self.nsrc, bs)]
 
-    def _solve(self, wn, b, mode):
-        u, info = S.solve(self.g, wn, b, mode=mode, opts=self._opts())
-        self.last_infos.append(info)
-        return u
+    def _levels(self, v_phys: torch.Tensor, freq: float):
+        """Multigrid levels of one frequency (solver "mlgmres"), else None."""
+        if self.cfg.solver == "cgmn":
+            return None
+        if self.cfg.solver != "mlgmres":
+            raise ValueError(f"unknown solver {self.cfg.solver!r}")
+        from . import multigrid as MG
+
+        npml = set(int(p) for p in self.geom.npml6)
+        if len(npml) != 1:
+            raise ValueError("the multigrid solver needs the same PML width on all faces")
+        v = v_phys.detach().to(torch.float64).cpu().numpy().reshape(self.geom.n)
+        return MG.build_levels(v, self.geom.d, npml.pop(), freq, self.geom.unit, device=self.dev)
+
+    def _solve(self, wn, b, mode, ml=None):
+        if ml is None:
+            u, info = S.solve(self.g, wn, b, mode=mode, opts=self._opts())
+            self.last_infos.append(info)
+            return u
+        from . import multigrid as MG
+
+        lv, R, P = ml
+        prec = "fp64" if str(self.cfg.precision).lower().startswith("fp") else "mixed"
+        out = torch.empty_like(b)
+        iters = []
+        for s in range(b.shape[0]):
+            if float(b[s].abs().max()) == 0.0:        # opAbstractMatrix.m:118
+                out[s].zero_()
+                continue
+            out[s], info = MG.solve(lv, R, P, b[s], tol=self.cfg.tol, maxit=self.cfg.maxit, mode=mode,
+                                    precision=prec)
+            iters.append(info["iters"])
+        self.last_infos.append({"iters": max(iters) if iters else 0, "solver": "mlgmres"})
+        return out
 
     # -- PDEfunc FORW_MODEL ----------------------------------------------------------------------
     def forward_model(self, v_phys: torch.Tensor, return_fields: bool = False):
@@ -209,8 +244,9 @@ class FWIProblem:
         cols, fields = [], []
         for k, fr in enumerate(self.geom.freqs):
             wn, _ = self._wavenumbers(v_phys, float(fr))
+            ml = self._levels(v_phys, float(fr))
             for srcs in self._batches():
-                U = self._solve(wn, self._sources(k, srcs), 1)
+                U = self._solve(wn, self._sources(k, srcs), 1, ml)
                 cols.append(self._sample(U))
                 if return_fields:
                     fields.append(U)
@@ -228,8 +264,9 @@ class FWIProblem:
         col = 0
         for k, fr in enumerate(self.geom.freqs):
             wn, _ = self._wavenumbers(v_phys, float(fr))
+            ml = self._levels(v_phys, float(fr))
             for srcs in self._batches():
-                U = self._solve(wn, self._sources(k, srcs), 1)
+                U = self._solve(wn, self._sources(k, srcs), 1, ml)
                 dpred = self._sample(U)
                 dobs = Dobs[:, col:col + len(srcs)].T.to(torch.complex128)
                 r = dpred - dobs                                     # LS_misfit.m:23
@@ -246,11 +283,12 @@ class FWIProblem:
         q = 0
         for k, fr in enumerate(self.geom.freqs):
             wn, dwn = self._wavenumbers(v_phys, float(fr))
+            ml = self._levels(v_phys, float(fr))
             for srcs in self._batches():
                 U = fields[q]
                 if U is None:
-                    U = self._solve(wn, self._sources(k, srcs), 1)   # recompute above the budget
-                V = self._solve(wn, self._spread(resid[q], -1.0), 2)   # H' \ (-Pr' dphi)
+                    U = self._solve(wn, self._sources(k, srcs), 1, ml)   # recompute above the budget
+                V = self._solve(wn, self._spread(resid[q], -1.0), 2, ml)   # H' \ (-Pr' dphi)
                 self._grad_accum(dwn, U, V, g)
                 q += 1
         return g

@@ -143,3 +143,26 @@ def test_jacobian_adjoint_and_gauss_newton(cuda):
     hgn = prob.hess_gn(mt, dmt)
     comp = prob.jacob_adj(mt, prob.jacob_forw(mt, dmt))
     assert (hgn - comp).abs().max().item() <= 1e-9 * comp.abs().max().item()
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_gradient_with_multigrid_solver_matches_oracle(cuda, precision):
+    """FWIConfig(solver="mlgmres"): forward and adjoint solves by FGMRES + ML_GMRES (the
+    reference's default for its 3D applications) give the oracle's (f, g) to solver tolerance."""
+    import torch
+    from h3d import fwi
+
+    geom, m0, mt = _geometry("s2/m2", freqs=(5.0,))
+    mod = _oracle_model(geom)
+    D_ref = slim_ref.pdefunc("forw_model", _flatF(mt), mod, geom.src_xyz, geom.src_amp, geom.rec_xyz,
+                             geom.freqs, tol=1e-10, maxit=20000, order=O.ORDER_COLOUR27, nthreads=1)
+    f_ref, g_ref = slim_ref.pdefunc("obj", _flatF(m0), mod, geom.src_xyz, geom.src_amp, geom.rec_xyz,
+                                    geom.freqs, Dobs=D_ref, tol=1e-10, maxit=20000,
+                                    order=O.ORDER_COLOUR27, nthreads=1)
+    prob = fwi.FWIProblem(geom, fwi.FWIConfig(tol=1e-10, precision=precision, solver="mlgmres"))
+    D = prob.forward_model(torch.as_tensor(mt, device=cuda)).cpu().numpy()
+    assert np.max(np.abs(D - D_ref)) <= 1e-6 * np.max(np.abs(D_ref))
+    f, g = prob.objective(torch.as_tensor(m0, device=cuda), torch.as_tensor(D_ref, device=cuda))
+    g = _flatF(g.cpu().numpy())
+    assert abs(f - f_ref) <= 1e-6 * abs(f_ref)
+    assert np.max(np.abs(g - g_ref)) <= 1e-5 * np.max(np.abs(g_ref))
