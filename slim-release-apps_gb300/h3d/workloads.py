@@ -57,24 +57,24 @@ def config2(order="block8", precision="mixed", freqs=None, nsrc=None, tol=1e-6, 
             "nsrc": len(srcs)}
 
 
-def config3_problem(precision="mixed", order="block8", nsrc=None, freqs=None):
+def config3_problem(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cgmn"):
     m = models.config3()
     meta = m.meta
     src = meta["src_xyz"] if nsrc is None else meta["src_xyz"][:nsrc]
     geom = fwi.Geometry(o=(0.0, 0.0, 0.0), d=m.h, n=m.n_phys, npml6=m.npml6, src_xyz=src,
                         rec_xyz=meta["rec_xyz"], freqs=meta["freqs"] if freqs is None else np.asarray(freqs),
                         f0=meta["f0"], t0=0.0, unit="s2/m2")
-    prob = fwi.FWIProblem(geom, fwi.FWIConfig(tol=1e-6, precision=precision, order=order))
+    prob = fwi.FWIProblem(geom, fwi.FWIConfig(tol=1e-6, precision=precision, order=order, solver=solver))
     m_true = torch.as_tensor(m.v ** -2.0, device=prob.dev)
     m0 = torch.as_tensor(meta["v0"] ** -2.0, device=prob.dev)
     return prob, m_true, m0
 
 
-def config3(precision="mixed", order="block8", nsrc=None, freqs=None):
+def config3(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cgmn"):
     """FWI gradient w.r.t. squared slowness: 32 jittered surface sources, 400 receivers,
     3 / 4.5 / 6 Hz on 161 x 161 x 81 (15-point PML); observed data modelled on the true
     model, gradient at the background model through the autograd function."""
-    prob, m_true, m0 = config3_problem(precision, order, nsrc, freqs)
+    prob, m_true, m0 = config3_problem(precision, order, nsrc, freqs, solver)
     Dobs = prob.forward_model(m_true)
     torch.cuda.synchronize()
     m = m0.clone().requires_grad_(True)
@@ -89,7 +89,7 @@ def config3(precision="mixed", order="block8", nsrc=None, freqs=None):
     pairs = prob.nsrc * len(prob.geom.freqs)
     return {"workload": "config3", "seconds": t, "grads_per_s": 1.0 / t, "pairs_per_s": pairs / t,
             "f": float(f.item()), "grad_norm": float(m.grad.norm().item()), "order": order,
-            "precision": precision, "nsrc": prob.nsrc, "freqs": [float(x) for x in prob.geom.freqs],
+            "precision": precision, "solver": solver, "nsrc": prob.nsrc, "freqs": [float(x) for x in prob.geom.freqs],
             "solves": len(prob.last_infos), "iters": [i["iters"] for i in prob.last_infos],
             "stored_wavefields": prob.wavefield_bytes() <= prob.cfg.hbm_budget_bytes}
 
@@ -130,12 +130,14 @@ def main(argv=None):
     ap.add_argument("--nsrc", type=int, default=None)
     ap.add_argument("--freqs", type=float, nargs="*", default=None)
     ap.add_argument("--nprob", type=int, default=48)
+    ap.add_argument("--solver", default="cgmn", choices=["cgmn", "mlgmres"])
     a = ap.parse_args(argv)
     t0 = time.time()
     if a.config == 2:
         out = config2(order=a.order or "block8", precision=a.precision, freqs=a.freqs, nsrc=a.nsrc)
     elif a.config == 3:
-        out = config3(precision=a.precision, order=a.order or "block8", nsrc=a.nsrc, freqs=a.freqs)
+        out = config3(precision=a.precision, order=a.order or "block8", nsrc=a.nsrc, freqs=a.freqs,
+                      solver=a.solver)
     else:
         out = config4(precision=a.precision, order=a.order or "colour27", nprob=a.nprob)
     out["wall_s"] = time.time() - t0
