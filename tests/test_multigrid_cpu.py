@@ -56,3 +56,25 @@ def test_ml_gmres_solves_small_helmholtz():
     r = b - levels[0].A(x)
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-6
     assert len(hst) - 1 <= 25
+
+
+def test_library_interpolation_weights_match_oracle():
+    """The library's host-side set-up (h3d.multigrid: cubic model coarsening and linear grid
+    transfer weights) against the oracle's restatement, on the grid pairs the levels use."""
+    import sys, os
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "slim-release-apps_gb300"))
+    from h3d import multigrid as MG
+
+    g = lambda m: np.linspace(0.0, 1.0, m)
+    for n, nc in ((61, 31), (201, 101), (101, 51), (29, 15), (16, 8)):
+        A = MG.cubic_weights(g(n), g(nc))
+        B = ML.cubic_interp_1d(g(n), g(nc)).toarray()
+        assert np.max(np.abs(A - B)) <= 1e-13
+        A = MG.linear_weights(g(nc), g(n))
+        B = ML.lin_interp_1d(g(nc), g(n)).toarray()
+        assert np.max(np.abs(A - B)) <= 1e-13
+    rng = np.random.default_rng(4)
+    v = rng.random((23, 19, 17)) + 1.0
+    f2c, _, ns = ML.fine2coarse(v.shape, (1.0, 1.0, 1.0), (2.0, 2.0, 2.0), "cubic")
+    ref = (f2c * v.reshape(-1, order="F")).reshape(ns, order="F")
+    assert np.max(np.abs(MG._coarsen_model(v, ns) - ref)) <= 1e-12
