@@ -107,7 +107,7 @@ typedef struct h3d_solve_opts {
     int32_t maxit;          /* default 10000 (LinSolveOpts.m:57); inner iterations cap */
     double w;               /* relaxation, default 1.5 (linearsolve.m:150) */
     int32_t precision;      /* h3d_precision */
-    int32_t order;          /* h3d_order */
+    int32_t order;          /* h3d_order, default BLOCK8 */
     int32_t stop_rule;      /* h3d_stop_rule */
     int32_t check_every;    /* iterations between host-visible convergence checks (graph length) */
     double inner_tol;       /* MIXED: relative tolerance of each complex64 inner solve */

@@ -78,7 +78,7 @@ void h3d_default_opts(h3d_solve_opts *o)
     o->maxit = 10000;
     o->w = 1.5;
     o->precision = H3D_PREC_FP64;
-    o->order = H3D_ORDER_COLOUR27;
+    o->order = H3D_ORDER_BLOCK8;
     o->stop_rule = H3D_STOP_TRUE_RESIDUAL;
     o->check_every = 25;
     o->inner_tol = 1e-3;

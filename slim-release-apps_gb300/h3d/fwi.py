@@ -121,7 +121,7 @@ class FWIConfig:
     tol: float = 1e-6
     maxit: int = 10000
     precision: str = "mixed"
-    order: str = "colour27"
+    order: str = "block8"
     hbm_budget_bytes: float = 40e9        # keep forward wavefields up to this size
     src_batch: int = 0                    # 0 = all sources of a frequency in one batch
     extra: dict = field(default_factory=dict)

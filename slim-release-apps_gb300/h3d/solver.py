@@ -35,7 +35,7 @@ def _mode(mode) -> int:
     return L.FORWARD if int(mode) == 1 else L.ADJOINT
 
 
-def make_opts(tol=1e-6, maxit=10000, precision="fp64", order="colour27", stop="true",
+def make_opts(tol=1e-6, maxit=10000, precision="fp64", order="block8", stop="true",
               inner_tol=None, max_outer=None, check_every=None, block=None, w=1.5,
               use_graphs=True, verbose=False, method="cgmn") -> L.SolveOpts:
     o = L.default_opts()

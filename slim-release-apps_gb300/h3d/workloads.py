@@ -94,7 +94,7 @@ def config3(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cg
             "stored_wavefields": prob.wavefield_bytes() <= prob.cfg.hbm_budget_bytes}
 
 
-def config4(precision="mixed", order="colour27", nprob=48):
+def config4(precision="mixed", order="block8", nprob=48):
     """48 problems with seeded sizes in [64, 192] per axis, 12.5 Hz, 1-16 sources each,
     solved in one batched call."""
     probs_m = models.config4(nprob=nprob)
@@ -139,7 +139,7 @@ def main(argv=None):
         out = config3(precision=a.precision, order=a.order or "block8", nsrc=a.nsrc, freqs=a.freqs,
                       solver=a.solver)
     else:
-        out = config4(precision=a.precision, order=a.order or "colour27", nprob=a.nprob)
+        out = config4(precision=a.precision, order=a.order or "block8", nprob=a.nprob)
     out["wall_s"] = time.time() - t0
     print(json.dumps(out), flush=True)
 
