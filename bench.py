@@ -68,7 +68,7 @@ def _sweep_kernel(order, variant):
                 else f"sweep_tile_kernel<float> (COLOUR27 colour phase, tile shape {variant})")
         return name, 54, TRAFFIC_PER_LAUNCH.get((order, variant))
     if order == "block8":
-        return f"sweep_block8_kernel<float> (BLOCK8 parity phase, configuration {variant})", 16, \
+        return f"sweep_block8_kernel<float> (BLOCK8 parity phase, configuration {variant})", 15, \
             TRAFFIC_PER_LAUNCH.get((order, variant))
     return f"{order} sweep", None, None
 

@@ -62,7 +62,7 @@ __global__ void __launch_bounds__(128) coef8_store_kernel(Op<T> op, cplx<T> *coe
 template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ, int R>
 __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_block8_kernel(
     Op<T> op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active, const T *rinv,
-    const cplx<T> *coef, int NI, int NJ, int NIp, int NJp, int par, int backward)
+    const cplx<T> *coef, int NI, int NJ, int NIp, int NJp, int par, int backward, int nsteps)
 {
     static_assert(BX % 3 == 0 && BY % 3 == 0 && BZ % 3 == 0, "block sides must be multiples of 3");
     constexpr int U = BX / 3, V = BY / 3, W = BZ / 3, NR = U * V * W, NT = NR * R;
@@ -97,6 +97,10 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_bloc
     const bool interior_block = !WNC && bi0 >= ilo[0] && min(bi0 + BX, op.nx) <= ihi[0] && bj0 >= ilo[1] &&
                                 min(bj0 + BY, op.ny) <= ihi[1] && bk0 >= ilo[2] && min(bk0 + BZ, op.nz) <= ihi[2];
     const bool stored = coef != nullptr && !interior_block;
+    // Colour of step s: the forward pass (q = 0..26), the backward pass (q = 26..0), or both in
+    // one launch (nsteps = 54: the last parity of the forward pass is the first of the backward
+    // pass, so one CTA runs the block's 27 colours up and then down)
+    auto colour_of = [&](int st) { return st < 27 ? (backward ? 26 - st : st) : 53 - st; };
     const cplx<T> *slab0 = stored ? coef + (size_t)((Ib + NI * (Jb + NJ * Kb)) * 27) * SLAB : nullptr;
     auto stage = [&](int q, int buf) {  // colour q's slab -> sc[buf], 16-byte copies
         constexpr int CH = SLAB * (int)sizeof(cplx<T>) / 16;
@@ -107,7 +111,7 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_bloc
 
     block_stage<T, WNC, PX, PY, NB, R, NT>(op, x, s0, act, i0, j0, k0, sx, swr, swi);
     if (stored) {
-        stage(backward ? 26 : 0, 0);
+        stage(colour_of(0), 0);
         asm volatile("cp.async.commit_group;\n" ::: "memory");
         asm volatile("cp.async.wait_group 0;\n" ::: "memory");
     }
@@ -134,16 +138,16 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_bloc
             if (bs) bv_n = bs[ctr];
         }
     };
-    fetch(backward ? 26 : 0);
-    for (int qq = 0; qq < 27; ++qq) {
-        const int q = backward ? 26 - qq : qq;
+    fetch(colour_of(0));
+    for (int qq = 0; qq < nsteps; ++qq) {
+        const int q = colour_of(qq);
         const T inv = inv_n;
         const cplx<T> bv = bv_n;
-        if (qq < 26) fetch(backward ? 25 - qq : qq + 1);
+        if (qq + 1 < nsteps) fetch(colour_of(qq + 1));
         if (stored) {
             // prefetch the next colour's coefficients into the other buffer (its previous
             // colour finished at the barrier that ended the last iteration)
-            if (qq < 26) stage(backward ? 25 - qq : qq + 1, (qq + 1) & 1);
+            if (qq + 1 < nsteps) stage(colour_of(qq + 1), (qq + 1) & 1);
             asm volatile("cp.async.commit_group;\n" ::: "memory");
             asm volatile("cp.async.wait_group 1;\n" ::: "memory");  // this colour's slab landed
             __syncthreads();
@@ -189,7 +193,7 @@ void block8_cfg_dims(int c, int32_t *blk, int *r)
 
 template <typename T, bool ADJ, bool WNC, int BX, int BY, int BZ, int R>
 static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active,
-                         const T *rinv, const cplx<T> *coef, bool backward, cudaStream_t st)
+                         const T *rinv, const cplx<T> *coef, cudaStream_t st)
 {
     constexpr size_t smem_box = block_smem<T, WNC, BX, BY, BZ, R>();
     constexpr size_t smem_coef = ((smem_box + 15) / 16) * 16 + 2 * sizeof(cplx<T>) * Coef8Layout<BX, BY, BZ>::SLAB;
@@ -222,10 +226,14 @@ static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs
             return H3D_ERR_BAD_ARG;
         }
         const dim3 grd((unsigned)nblk, ngrp);
-        for (int pp = 0; pp < 8; ++pp) {
-            const int par = backward ? 7 - pp : pp;
+        // forward pass: parities 0..6, then parity 7 up and down in one launch, then the
+        // backward pass: parities 6..0 -- 15 launches per double sweep
+        for (int pp = 0; pp < 15; ++pp) {
+            const int par = pp < 8 ? pp : 14 - pp;
+            const int bw = pp < 8 ? 0 : 1;
+            const int nsteps = pp == 7 ? 54 : 27;
             sweep_block8_kernel<T, ADJ, WNC, BX, BY, BZ, R><<<grd, NT, smem, st>>>(
-                op, x, b, nrhs, w, active, rinv, coef, NI, NJ, NIp, NJp, par, backward ? 1 : 0);
+                op, x, b, nrhs, w, active, rinv, coef, NI, NJ, NIp, NJp, par, bw, nsteps);
         }
         H3D_CUDA_TRY(cudaGetLastError());
         return H3D_OK;
@@ -234,14 +242,14 @@ static int block8_pass_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs
 
 template <typename T, bool ADJ, bool WNC>
 static int block8_pass_cfg(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, const int *active,
-                           const T *rinv, const cplx<T> *coef, int cfg, bool backward, cudaStream_t st)
+                           const T *rinv, const cplx<T> *coef, int cfg, cudaStream_t st)
 {
     // the stored layout is the 12x12x12 one: the 24x12x12 configuration forms coefficients itself
     switch (cfg) {
-    case 1: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 2>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
-    case 2: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 4>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
-    case 3: return block8_pass_t<T, ADJ, WNC, 24, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, nullptr, backward, st);
-    default: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, coef, backward, st);
+    case 1: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 2>(op, x, b, nrhs, w, active, rinv, coef, st);
+    case 2: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 4>(op, x, b, nrhs, w, active, rinv, coef, st);
+    case 3: return block8_pass_t<T, ADJ, WNC, 24, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, nullptr, st);
+    default: return block8_pass_t<T, ADJ, WNC, 12, 12, 12, 1>(op, x, b, nrhs, w, active, rinv, coef, st);
     }
 }
 
@@ -308,15 +316,12 @@ int sweep_block8(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs, T w, c
         if (rc) return rc;
         rinv = norms.as<T>();
     }
-    for (int pass = 0; pass < 2; ++pass) {
-        const bool bw = pass == 1;
-        int rc;
-        if (!adj && !wnc) rc = block8_pass_cfg<T, false, false>(op, x, b, nrhs, w, active, rinv, coef, cfg, bw, st);
-        else if (!adj && wnc) rc = block8_pass_cfg<T, false, true>(op, x, b, nrhs, w, active, rinv, coef, cfg, bw, st);
-        else if (adj && !wnc) rc = block8_pass_cfg<T, true, false>(op, x, b, nrhs, w, active, rinv, coef, cfg, bw, st);
-        else rc = block8_pass_cfg<T, true, true>(op, x, b, nrhs, w, active, rinv, coef, cfg, bw, st);
-        if (rc) return rc;
-    }
+    int rc;
+    if (!adj && !wnc) rc = block8_pass_cfg<T, false, false>(op, x, b, nrhs, w, active, rinv, coef, cfg, st);
+    else if (!adj && wnc) rc = block8_pass_cfg<T, false, true>(op, x, b, nrhs, w, active, rinv, coef, cfg, st);
+    else if (adj && !wnc) rc = block8_pass_cfg<T, true, false>(op, x, b, nrhs, w, active, rinv, coef, cfg, st);
+    else rc = block8_pass_cfg<T, true, true>(op, x, b, nrhs, w, active, rinv, coef, cfg, st);
+    if (rc) return rc;
     return H3D_OK;
 }
 

@@ -204,7 +204,7 @@ struct CgRun {
             return 2 * (((op.nx + bx - 1) / bx - 1) + 2 * ((op.ny + by - 1) / by - 1) +
                         4 * ((op.nz + bz - 1) / bz - 1) + 1);
         }
-        if (order == H3D_ORDER_BLOCK8) return 16;
+        if (order == H3D_ORDER_BLOCK8) return 15;
         int n = 0;
         for (int q = 0; q < 27; ++q) {
             const int a = q % 3, bq = (q / 3) % 3, cq = q / 9;
