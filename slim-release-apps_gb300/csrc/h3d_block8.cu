@@ -97,6 +97,9 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_bloc
     const bool interior_block = !WNC && bi0 >= ilo[0] && min(bi0 + BX, op.nx) <= ihi[0] && bj0 >= ilo[1] &&
                                 min(bj0 + BY, op.ny) <= ihi[1] && bk0 >= ilo[2] && min(bk0 + BZ, op.nz) <= ihi[2];
     const bool stored = coef != nullptr && !interior_block;
+    // the block holds a row on a face of the grid (CTA-uniform): its scatter is masked
+    const bool edge_block = bi0 == 0 || bj0 == 0 || bk0 == 0 || bi0 + BX >= op.nx || bj0 + BY >= op.ny ||
+                            bk0 + BZ >= op.nz;
     // Colour of step s: the forward pass (q = 0..26), the backward pass (q = 26..0), or both in
     // one launch (nsteps = 54: the last parity of the forward pass is the first of the backward
     // pass, so one CTA runs the block's 27 colours up and then down)
@@ -156,8 +159,10 @@ __global__ void __launch_bounds__((BX / 3) * (BY / 3) * (BZ / 3) * R) sweep_bloc
         const int i = bi0 + a + 3 * u, j = bj0 + bq + 3 * v, k = bk0 + cq + 3 * ww;
         if (mine && i < op.nx && j < op.ny && k < op.nz) {
             const int lc = (1 + a + 3 * u) + PX * ((1 + bq + 3 * v) + PY * (1 + cq + 3 * ww));
-            if (stored)
-                block_row_stored<T, PX, PY>(op, bx, sc + (qq & 1) * SLAB, NR, row, bv, inv, w, i, j, k, lc);
+            if (stored && edge_block)
+                block_row_stored<T, PX, PY, true>(op, bx, sc + (qq & 1) * SLAB, NR, row, bv, inv, w, i, j, k, lc);
+            else if (stored)
+                block_row_stored<T, PX, PY, false>(op, bx, sc + (qq & 1) * SLAB, NR, row, bv, inv, w, i, j, k, lc);
             else
                 block_row<T, ADJ, WNC, PX, PY>(op, bx, swr, swi, bv, inv, w, i, j, k, lc);
         }

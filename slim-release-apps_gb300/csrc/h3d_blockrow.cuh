@@ -111,18 +111,16 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
 #define H3D_GI(t, dx, dy, dz)                                                                  \
     {                                                                                          \
         const cplx<T> xv = bx[lc + dx + PX * (dy + PY * dz)];                                  \
-        acc[dz + 1].re += cr[t] * xv.re;                                                       \
-        acc[dz + 1].im += cr[t] * xv.im;                                                       \
+        fma_rc(acc[dz + 1], cr[t], xv);                                                        \
     }
         H3D_FOR_27(H3D_GI)
 #undef H3D_GI
-        const cplx<T> atx = (acc[0] + acc[1]) + acc[2];
+        const cplx<T> atx = cadd(cadd(acc[0], acc[1]), acc[2]);
         const cplx<T> d = (w * inv) * (bv - atx);
 #define H3D_SI(t, dx, dy, dz)                                                                  \
     {                                                                                          \
         cplx<T> &o = bx[lc + dx + PX * (dy + PY * dz)];                                        \
-        o.re += d.re * cr[t];                                                                  \
-        o.im += d.im * cr[t];                                                                  \
+        fma_rc(o, cr[t], d);                                                                   \
     }
         H3D_FOR_27(H3D_SI)
 #undef H3D_SI
@@ -135,22 +133,21 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
 #define H3D_CC(t, dx, dy, dz) c[t] = coef_at<t, dx, dy, dz, T, ADJ, false, WNC>(op, pml, ADJ ? 0x7ffffffu : m, wnf);
         H3D_FOR_27(H3D_CC)
 #undef H3D_CC
-        cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+        const cplx<T> z = mk<T>(T(0), T(0));
+        CSum<T> acc[3] = {csum_init(z), csum_init(z), csum_init(z)};
 #define H3D_GC(t, dx, dy, dz)                                                                  \
     {                                                                                          \
         const cplx<T> xv = bx[lc + dx + PX * (dy + PY * dz)];                                  \
-        acc[dz + 1].re += c[t].re * xv.re - c[t].im * xv.im;                                   \
-        acc[dz + 1].im += c[t].re * xv.im + c[t].im * xv.re;                                   \
+        csum_mac(acc[dz + 1], c[t], xv);                                                       \
     }
         H3D_FOR_27(H3D_GC)
 #undef H3D_GC
-        const cplx<T> atx = (acc[0] + acc[1]) + acc[2];
-        const cplx<T> d = (w * inv) * (bv - atx);
+        const cplx<T> atx = cadd(cadd(csum_value(acc[0]), csum_value(acc[1])), csum_value(acc[2]));
+        const Scat<T> sd = scat_of((w * inv) * (bv - atx));
 #define H3D_SC(t, dx, dy, dz)                                                                  \
     if (m & (1u << t)) {                                                                       \
         cplx<T> &o = bx[lc + dx + PX * (dy + PY * dz)];                                        \
-        o.re += d.re * c[t].re + d.im * c[t].im;                                               \
-        o.im += d.im * c[t].re - d.re * c[t].im;                                               \
+        scat_mac(o, sd, c[t]);                                                                 \
     }
         H3D_FOR_27(H3D_SC)
 #undef H3D_SC
@@ -158,32 +155,35 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
 }
 
 // Project row (i, j, k) with its 27 coefficients read from shared memory (sc[t * NR + row],
-// staged from the stored coefficients).  Neighbours outside the grid are masked as above.
-template <typename T, int PX, int PY>
+// staged from the stored coefficients).  Neighbours outside the grid are masked as above;
+// EDGE = false: the caller's block has no row on a face of the grid, nothing is masked.
+template <typename T, int PX, int PY, bool EDGE>
 __device__ __forceinline__ void block_row_stored(const Op<T> &op, cplx<T> *bx, const cplx<T> *sc, int NR, int row,
                                                  cplx<T> bv, T inv, T w, int i, int j, int k, int lc)
 {
-    const bool edge = i == 0 || j == 0 || k == 0 || i == op.nx - 1 || j == op.ny - 1 || k == op.nz - 1;
-    const uint32_t m = edge ? inside_mask(i, j, k, op.nx, op.ny, op.nz) : 0x7ffffffu;
+    uint32_t m = 0x7ffffffu;
+    if constexpr (EDGE) {
+        const bool edge = i == 0 || j == 0 || k == 0 || i == op.nx - 1 || j == op.ny - 1 || k == op.nz - 1;
+        if (edge) m = inside_mask(i, j, k, op.nx, op.ny, op.nz);
+    }
     cplx<T> c[27];
 #pragma unroll
     for (int t = 0; t < 27; ++t) c[t] = sc[t * NR + row];
-    cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+    const cplx<T> z = mk<T>(T(0), T(0));
+    CSum<T> acc[3] = {csum_init(z), csum_init(z), csum_init(z)};
 #define H3D_GS(t, dx, dy, dz)                                                                  \
     {                                                                                          \
         const cplx<T> xv = bx[lc + dx + PX * (dy + PY * dz)];                                  \
-        acc[dz + 1].re += c[t].re * xv.re - c[t].im * xv.im;                                   \
-        acc[dz + 1].im += c[t].re * xv.im + c[t].im * xv.re;                                   \
+        csum_mac(acc[dz + 1], c[t], xv);                                                       \
     }
     H3D_FOR_27(H3D_GS)
 #undef H3D_GS
-    const cplx<T> atx = (acc[0] + acc[1]) + acc[2];
-    const cplx<T> d = (w * inv) * (bv - atx);
+    const cplx<T> atx = cadd(cadd(csum_value(acc[0]), csum_value(acc[1])), csum_value(acc[2]));
+    const Scat<T> sd = scat_of((w * inv) * (bv - atx));
 #define H3D_SS(t, dx, dy, dz)                                                                  \
     if (m & (1u << t)) {                                                                       \
         cplx<T> &o = bx[lc + dx + PX * (dy + PY * dz)];                                        \
-        o.re += d.re * c[t].re + d.im * c[t].im;                                               \
-        o.im += d.im * c[t].re - d.re * c[t].im;                                               \
+        scat_mac(o, sd, c[t]);                                                                 \
     }
     H3D_FOR_27(H3D_SS)
 #undef H3D_SS

@@ -36,12 +36,122 @@ template <typename T>
 __host__ __device__ __forceinline__ cplx<T> cconj(cplx<T> a) { return {a.re, -a.im}; }
 template <typename T>
 __host__ __device__ __forceinline__ T cabs2(cplx<T> a) { return a.re * a.re + a.im * a.im; }
-// acc += a * b
+// acc += a * b as four chained multiply-adds (written one product per statement so that
+// each contracts into one FMA; `acc += p - q` would cost a multiply, an FMA and an add)
 template <typename T>
 __host__ __device__ __forceinline__ void cmac(cplx<T> &acc, cplx<T> a, cplx<T> b)
 {
-    acc.re += a.re * b.re - a.im * b.im;
-    acc.im += a.re * b.im + a.im * b.re;
+    acc.re += a.re * b.re;
+    acc.re -= a.im * b.im;
+    acc.im += a.re * b.im;
+    acc.im += a.im * b.re;
+}
+// acc += a * conj(b)
+template <typename T>
+__host__ __device__ __forceinline__ void cmac_cb(cplx<T> &acc, cplx<T> a, cplx<T> b)
+{
+    acc.re += a.re * b.re;
+    acc.re += a.im * b.im;
+    acc.im += a.im * b.re;
+    acc.im -= a.re * b.im;
+}
+
+// ---------------------------------------------------------------------------------------
+// Packed complex64 arithmetic.  sm_100-class GPUs execute an FP32 add / multiply / FMA on
+// a register pair as one instruction (add.f32x2, fma.rn.f32x2), each component rounded
+// exactly like the scalar operation, and take a scalar register or constant as a
+// broadcast operand.  A complex value times a real scalar is then one instruction, and a
+// complex-by-complex product accumulates as two: P += a.re * b and Q += a.im * b, the
+// product sum being (P.re - Q.im, P.im + Q.re).  Complex128 keeps the scalar forms.
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+#define H3D_F32X2 1
+#else
+#define H3D_F32X2 0
+#endif
+
+// acc += s * v (s real)
+template <typename T>
+__device__ __forceinline__ void fma_rc(cplx<T> &acc, T s, cplx<T> v)
+{
+    acc.re += s * v.re;
+    acc.im += s * v.im;
+}
+// a + b
+template <typename T>
+__device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) { return a + b; }
+// s * v (s real)
+template <typename T>
+__device__ __forceinline__ cplx<T> cscale(T s, cplx<T> v) { return s * v; }
+#if H3D_F32X2
+__device__ __forceinline__ float2 f2_of(cplx<float> a) { return make_float2(a.re, a.im); }
+template <>
+__device__ __forceinline__ void fma_rc<float>(cplx<float> &acc, float s, cplx<float> v)
+{
+    const float2 r = __ffma2_rn(make_float2(s, s), f2_of(v), f2_of(acc));
+    acc = cplx<float>{r.x, r.y};
+}
+template <>
+__device__ __forceinline__ cplx<float> cadd<float>(cplx<float> a, cplx<float> b)
+{
+    const float2 r = __fadd2_rn(f2_of(a), f2_of(b));
+    return cplx<float>{r.x, r.y};
+}
+template <>
+__device__ __forceinline__ cplx<float> cscale<float>(float s, cplx<float> v)
+{
+    const float2 r = __fmul2_rn(make_float2(s, s), f2_of(v));
+    return cplx<float>{r.x, r.y};
+}
+#endif
+
+// A running sum of complex products.  Complex128: one accumulator, chained FMAs (cmac).
+// Complex64: the two packed partial sums described above.
+template <typename T>
+struct CSum {
+    cplx<T> p, q;
+};
+template <typename T>
+__device__ __forceinline__ CSum<T> csum_init(cplx<T> v0) { return CSum<T>{v0, mk<T>(T(0), T(0))}; }
+template <typename T>
+__device__ __forceinline__ void csum_mac(CSum<T> &s, cplx<T> a, cplx<T> b)
+{
+    if constexpr (sizeof(T) == 4) {
+        fma_rc(s.p, a.re, b);
+        fma_rc(s.q, a.im, b);
+    } else {
+        cmac(s.p, a, b);
+    }
+}
+// s += conj(a) * b
+template <typename T>
+__device__ __forceinline__ void csum_mac_ca(CSum<T> &s, cplx<T> a, cplx<T> b)
+{
+    if constexpr (sizeof(T) == 4) {
+        fma_rc(s.p, a.re, b);
+        fma_rc(s.q, -a.im, b);
+    } else {
+        cmac(s.p, cconj(a), b);
+    }
+}
+template <typename T>
+__device__ __forceinline__ cplx<T> csum_value(const CSum<T> &s)
+{
+    if constexpr (sizeof(T) == 4) return mk<T>(s.p.re - s.q.im, s.p.im + s.q.re);
+    else return s.p;
+}
+// acc += d * conj(c), the Kaczmarz scatter: c.re (d.re, d.im) + c.im (d.im, -d.re), two
+// packed FMAs with the pairs (d.re, d.im) and (d.im, -d.re) formed once per row
+template <typename T>
+struct Scat {
+    cplx<T> d1, d2;
+};
+template <typename T>
+__device__ __forceinline__ Scat<T> scat_of(cplx<T> d) { return Scat<T>{d, mk<T>(d.im, -d.re)}; }
+template <typename T>
+__device__ __forceinline__ void scat_mac(cplx<T> &o, const Scat<T> &s, cplx<T> c)
+{
+    fma_rc(o, c.re, s.d1);
+    fma_rc(o, c.im, s.d2);
 }
 
 // Stencil weights W1..W3, WM1..WM4 (Helm3d_27pt.h:194-200).

@@ -22,7 +22,7 @@ template <typename T, bool WNC>
 __device__ __forceinline__ cplx<T> wmul(cplx<T> w, cplx<T> v)
 {
     if constexpr (WNC) return w * v;
-    else return mk<T>(w.re * v.re, w.re * v.im);
+    else return cscale(w.re, v);
 }
 
 template <typename T, bool ADJ, bool WNC, int PITCH>
@@ -41,21 +41,33 @@ __device__ __forceinline__ PlaneSums<T> plane_sums(const cplx<T> *sxp, const T *
     p.fxp = X(1, 0);
     p.fym = X(0, -1);
     p.fyp = X(0, 1);
-    p.cxm = mm + mp;
-    p.cxp = pm + pp;
-    p.cym = mm + pm;
-    p.cyp = mp + pp;
+    p.cxm = cadd(mm, mp);
+    p.cxp = cadd(pm, pp);
+    p.cym = cadd(mm, pm);
+    p.cyp = cadd(mp, pp);
     if constexpr (!ADJ) {
         p.wm = wmul<T, WNC>(W(0, 0), p.m);
-        p.wfx = wmul<T, WNC>(W(-1, 0), p.fxm) + wmul<T, WNC>(W(1, 0), p.fxp);
-        p.wfy = wmul<T, WNC>(W(0, -1), p.fym) + wmul<T, WNC>(W(0, 1), p.fyp);
-        p.wc4 = wmul<T, WNC>(W(-1, -1), mm) + wmul<T, WNC>(W(-1, 1), mp) + wmul<T, WNC>(W(1, -1), pm) +
-                wmul<T, WNC>(W(1, 1), pp);
+        if constexpr (WNC) {
+            p.wfx = wmul<T, WNC>(W(-1, 0), p.fxm) + wmul<T, WNC>(W(1, 0), p.fxp);
+            p.wfy = wmul<T, WNC>(W(0, -1), p.fym) + wmul<T, WNC>(W(0, 1), p.fyp);
+            p.wc4 = wmul<T, WNC>(W(-1, -1), mm) + wmul<T, WNC>(W(-1, 1), mp) + wmul<T, WNC>(W(1, -1), pm) +
+                    wmul<T, WNC>(W(1, 1), pp);
+        } else {
+            // real wavenumber: products then accumulated one FMA each
+            p.wfx = cscale(W(-1, 0).re, p.fxm);
+            fma_rc(p.wfx, W(1, 0).re, p.fxp);
+            p.wfy = cscale(W(0, -1).re, p.fym);
+            fma_rc(p.wfy, W(0, 1).re, p.fyp);
+            p.wc4 = cscale(W(-1, -1).re, mm);
+            fma_rc(p.wc4, W(-1, 1).re, mp);
+            fma_rc(p.wc4, W(1, -1).re, pm);
+            fma_rc(p.wc4, W(1, 1).re, pp);
+        }
     } else {
         p.wm = p.m;
-        p.wfx = p.fxm + p.fxp;
-        p.wfy = p.fym + p.fyp;
-        p.wc4 = p.cxm + p.cxp;
+        p.wfx = cadd(p.fxm, p.fxp);
+        p.wfy = cadd(p.fym, p.fyp);
+        p.wc4 = cadd(p.cxm, p.cxp);
     }
     return p;
 }
@@ -78,13 +90,6 @@ __device__ __forceinline__ void acc_zero(RowAcc<T> &a)
     a.mass = a.bxm = a.bxp = a.bym = a.byp = a.bzm = a.bzp = a.bsx = a.bsy = a.bsz = z;
 }
 
-template <typename T>
-__device__ __forceinline__ void fma_rc(cplx<T> &acc, T s, cplx<T> v)
-{
-    acc.re += s * v.re;
-    acc.im += s * v.im;
-}
-
 // ROLE: 0 = the plane below the row (k-1), 1 = the row's plane, 2 = the plane above.
 template <int ROLE, typename T, bool DERIV>
 __device__ __forceinline__ void acc_plane(RowAcc<T> &a, const PlaneSums<T> &P, const Op<T> &op)
@@ -92,15 +97,15 @@ __device__ __forceinline__ void acc_plane(RowAcc<T> &a, const PlaneSums<T> &P, c
     const T w3 = op.w3a2;
     if constexpr (ROLE == 1) {
         fma_rc(a.mass, op.wn_c, P.wm);
-        fma_rc(a.mass, T(-kWM2), P.wfx + P.wfy);
+        fma_rc(a.mass, T(-kWM2), cadd(P.wfx, P.wfy));
         fma_rc(a.mass, T(-kWM3), P.wc4);
     } else {
         fma_rc(a.mass, T(-kWM2), P.wm);
-        fma_rc(a.mass, T(-kWM3), P.wfx + P.wfy);
+        fma_rc(a.mass, T(-kWM3), cadd(P.wfx, P.wfy));
         fma_rc(a.mass, T(-kWM4), P.wc4);
     }
     if constexpr (!DERIV) {
-        const cplx<T> fx = P.fxm + P.fxp, fy = P.fym + P.fyp, c4 = P.cxm + P.cxp;
+        const cplx<T> fx = cadd(P.fxm, P.fxp), fy = cadd(P.fym, P.fyp), c4 = cadd(P.cxm, P.cxp);
         if constexpr (ROLE == 1) {
             fma_rc(a.bxm, op.pml_x, P.fxm); fma_rc(a.bxm, -op.xy, P.cxm);
             fma_rc(a.bxp, op.pml_x, P.fxp); fma_rc(a.bxp, -op.xy, P.cxp);
@@ -128,18 +133,23 @@ template <typename T, bool ADJ, bool DERIV, bool WNC>
 __device__ __forceinline__ cplx<T> acc_finish(const RowAcc<T> &a, const RowPml<T> &p, cplx<T> wc)
 {
     cplx<T> y = a.mass;
-    if constexpr (ADJ) y = WNC ? cconj(wc) * y : mk<T>(wc.re * y.re, wc.re * y.im);
+    if constexpr (ADJ) y = WNC ? cconj(wc) * y : cscale(wc.re, y);
     if constexpr (!DERIV) {
-        auto f = [&](cplx<T> v) { return ADJ ? cconj(v) : v; };
-        cmac(y, f(p.Axm), a.bxm);
-        cmac(y, f(p.Axp), a.bxp);
-        cmac(y, f(p.Aym), a.bym);
-        cmac(y, f(p.Ayp), a.byp);
-        cmac(y, f(p.Azm), a.bzm);
-        cmac(y, f(p.Azp), a.bzp);
-        cmac(y, f(p.Sx), a.bsx);
-        cmac(y, f(p.Sy), a.bsy);
-        cmac(y, f(p.Sz), a.bsz);
+        CSum<T> s = csum_init(y);
+        auto mac = [&](cplx<T> f, cplx<T> br) {
+            if constexpr (ADJ) csum_mac_ca(s, f, br);
+            else csum_mac(s, f, br);
+        };
+        mac(p.Axm, a.bxm);
+        mac(p.Axp, a.bxp);
+        mac(p.Aym, a.bym);
+        mac(p.Ayp, a.byp);
+        mac(p.Azm, a.bzm);
+        mac(p.Azp, a.bzp);
+        mac(p.Sx, a.bsx);
+        mac(p.Sy, a.bsy);
+        mac(p.Sz, a.bsz);
+        y = csum_value(s);
     }
     return y;
 }
@@ -153,14 +163,14 @@ __device__ __forceinline__ void acc_plane_xy(RowAcc<T> &a, const PlaneSums<T> &P
 {
     if constexpr (ROLE == 1) {
         fma_rc(a.mass, op.wn_c, P.wm);
-        fma_rc(a.mass, T(-kWM2), P.wfx + P.wfy);
+        fma_rc(a.mass, T(-kWM2), cadd(P.wfx, P.wfy));
         fma_rc(a.mass, T(-kWM3), P.wc4);
     } else {
         fma_rc(a.mass, T(-kWM2), P.wm);
-        fma_rc(a.mass, T(-kWM3), P.wfx + P.wfy);
+        fma_rc(a.mass, T(-kWM3), cadd(P.wfx, P.wfy));
         fma_rc(a.mass, T(-kWM4), P.wc4);
     }
-    const cplx<T> fx = P.fxm + P.fxp, fy = P.fym + P.fyp, c4 = P.cxm + P.cxp;
+    const cplx<T> fx = cadd(P.fxm, P.fxp), fy = cadd(P.fym, P.fyp), c4 = cadd(P.cxm, P.cxp);
     cplx<T> &r = a.bsx;
     if constexpr (ZI) {
         if constexpr (ROLE == 1) {
@@ -186,13 +196,18 @@ template <typename T, bool ADJ, bool ZI>
 __device__ __forceinline__ cplx<T> acc_finish_xy(const RowAcc<T> &a, const RowPml<T> &p, cplx<T> wc)
 {
     cplx<T> y = a.mass;
-    if constexpr (ADJ) y = mk<T>(wc.re * y.re, wc.re * y.im);
-    y = y + a.bsx;
+    if constexpr (ADJ) y = cscale(wc.re, y);
+    y = cadd(y, a.bsx);
     if constexpr (!ZI) {
-        auto f = [&](cplx<T> v) { return ADJ ? cconj(v) : v; };
-        cmac(y, f(p.Azm), a.bzm);
-        cmac(y, f(p.Azp), a.bzp);
-        cmac(y, f(p.Sz), a.bsz);
+        CSum<T> s = csum_init(y);
+        auto mac = [&](cplx<T> f, cplx<T> br) {
+            if constexpr (ADJ) csum_mac_ca(s, f, br);
+            else csum_mac(s, f, br);
+        };
+        mac(p.Azm, a.bzm);
+        mac(p.Azp, a.bzp);
+        mac(p.Sz, a.bsz);
+        y = csum_value(s);
     }
     return y;
 }

@@ -131,20 +131,17 @@ __global__ void __launch_bounds__(128) sweep_direct_kernel(Op<T> op, cplx<T> *x,
         H3D_FOR_27(H3D_DG)
 #undef H3D_DG
         // one partial sum per plane dz, each in offset order
-        cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+        const cplx<T> z = mk<T>(T(0), T(0));
+        CSum<T> acc[3] = {csum_init(z), csum_init(z), csum_init(z)};
 #pragma unroll
-        for (int t = 0; t < 27; ++t) {
-            acc[t / 9].re += c[t].re * xv[t].re - c[t].im * xv[t].im;
-            acc[t / 9].im += c[t].re * xv[t].im + c[t].im * xv[t].re;
-        }
-        const cplx<T> atx = (acc[0] + acc[1]) + acc[2];
+        for (int t = 0; t < 27; ++t) csum_mac(acc[t / 9], c[t], xv[t]);
+        const cplx<T> atx = cadd(cadd(csum_value(acc[0]), csum_value(acc[1])), csum_value(acc[2]));
         const cplx<T> bv = b ? b[(long long)s * op.N + ctr] : mk<T>(T(0), T(0));
-        const cplx<T> d = (w * inv) * (bv - atx);
+        const Scat<T> sd = scat_of((w * inv) * (bv - atx));
 #define H3D_DS(t, dx, dy, dz)                                                                  \
     if ((m >> t) & 1u) {                                                                       \
         cplx<T> o = xv[t];                                                                     \
-        o.re += d.re * c[t].re + d.im * c[t].im;                                               \
-        o.im += d.im * c[t].re - d.re * c[t].im;                                               \
+        scat_mac(o, sd, c[t]);                                                                 \
         xs[dx + op.sy * dy + op.sz * dz] = o;                                                  \
     }
         H3D_FOR_27(H3D_DS)

@@ -161,8 +161,7 @@ __global__ void __launch_bounds__(TU *TV *TW, MINB) sweep_tile_kernel(Op<T> op, 
 #define H3D_GI(t, dx, dy, dz)                                                                  \
     {                                                                                          \
         const cplx<T> xv = sx[lc + dx + PX * (dy + BY * dz)];                                  \
-        acc[dz + 1].re += cr[t] * xv.re;                                                       \
-        acc[dz + 1].im += cr[t] * xv.im;                                                       \
+        fma_rc(acc[dz + 1], cr[t], xv);                                                        \
     }
             H3D_FOR_27(H3D_GI)
 #undef H3D_GI
@@ -172,8 +171,7 @@ __global__ void __launch_bounds__(TU *TV *TW, MINB) sweep_tile_kernel(Op<T> op, 
 #define H3D_SI(t, dx, dy, dz)                                                                  \
     {                                                                                          \
         cplx<T> &o = sx[lc + dx + PX * (dy + BY * dz)];                                        \
-        o.re += d.re * cr[t];                                                                  \
-        o.im += d.im * cr[t];                                                                  \
+        fma_rc(o, cr[t], d);                                                                   \
     }
             H3D_FOR_27(H3D_SI)
 #undef H3D_SI
@@ -197,23 +195,22 @@ __global__ void __launch_bounds__(TU *TV *TW, MINB) sweep_tile_kernel(Op<T> op, 
                 for (int t = 0; t < 27; ++t) nrm += cabs2(c[t]);
                 inv = T(1) / nrm;
             }
-            cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+            const cplx<T> z = mk<T>(T(0), T(0));
+            CSum<T> acc[3] = {csum_init(z), csum_init(z), csum_init(z)};
 #define H3D_GC(t, dx, dy, dz)                                                                  \
     {                                                                                          \
         const cplx<T> xv = sx[lc + dx + PX * (dy + BY * dz)];                                  \
-        acc[dz + 1].re += c[t].re * xv.re - c[t].im * xv.im;                                   \
-        acc[dz + 1].im += c[t].re * xv.im + c[t].im * xv.re;                                   \
+        csum_mac(acc[dz + 1], c[t], xv);                                                       \
     }
             H3D_FOR_27(H3D_GC)
 #undef H3D_GC
-        const cplx<T> atx = (acc[0] + acc[1]) + acc[2];
+            const cplx<T> atx = cadd(cadd(csum_value(acc[0]), csum_value(acc[1])), csum_value(acc[2]));
             const cplx<T> bv = bs ? bs[ctr] : mk<T>(T(0), T(0));
-            const cplx<T> d = (w * inv) * (bv - atx);
+            const Scat<T> sd = scat_of((w * inv) * (bv - atx));
 #define H3D_SC(t, dx, dy, dz)                                                                  \
     {                                                                                          \
         cplx<T> &o = sx[lc + dx + PX * (dy + BY * dz)];                                        \
-        o.re += d.re * c[t].re + d.im * c[t].im;                                               \
-        o.im += d.im * c[t].re - d.re * c[t].im;                                               \
+        scat_mac(o, sd, c[t]);                                                                 \
     }
             H3D_FOR_27(H3D_SC)
 #undef H3D_SC
