@@ -12,6 +12,7 @@
 #include <vector>
 
 #include "h3d_internal.cuh"
+#include "h3d_kernels.cuh"
 
 namespace h3d {
 
@@ -159,6 +160,7 @@ static int make_op(const h3d_grid *g, const T *wn, const T *wni, Op<T> *op)
 {
     int rc = check_grid(g);
     if (rc) return rc;
+    mvp_prime_occupancy();
     TabEntry e;
     rc = get_tables<T>(g, &e);
     if (rc) return rc;
@@ -260,6 +262,7 @@ int make_op_f64_at(const h3d_grid *g, const double *wn, const double *wni, const
 {
     int rc = check_grid(g);
     if (rc) return rc;
+    mvp_prime_occupancy();
     std::vector<std::complex<double>> tab;
     Op<double> o{};
     fill_tables(g, tab, o.lo, o.hi, o.sum);

@@ -60,75 +60,84 @@ __host__ __device__ __forceinline__ void cmac_cb(cplx<T> &acc, cplx<T> a, cplx<T
 // Packed complex64 arithmetic.  sm_100-class GPUs execute an FP32 add / multiply / FMA on
 // a register pair as one instruction (add.f32x2, fma.rn.f32x2), each component rounded
 // exactly like the scalar operation, and take a scalar register or constant as a
-// broadcast operand.  A complex value times a real scalar is then one instruction, and a
-// complex-by-complex product accumulates as two: P += a.re * b and Q += a.im * b, the
-// product sum being (P.re - Q.im, P.im + Q.re).  Complex128 keeps the scalar forms.
+// broadcast operand.  A complex value times a real scalar is then one instruction.  The
+// packed forms pay off in issue-bound kernels (the matvec); the latency-bound Kaczmarz
+// sweeps measured slower with them and keep the scalar forms.  PK selects the packed form
+// (complex64 on sm_100+ only; complex128 is always scalar).
 #if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
 #define H3D_F32X2 1
 #else
 #define H3D_F32X2 0
 #endif
 
-// acc += s * v (s real)
 template <typename T>
+__device__ __forceinline__ float2 f2_of(cplx<T> a) { return make_float2(a.re, a.im); }
+
+// acc += s * v (s real)
+template <bool PK = false, typename T>
 __device__ __forceinline__ void fma_rc(cplx<T> &acc, T s, cplx<T> v)
 {
+#if H3D_F32X2
+    if constexpr (PK && sizeof(T) == 4) {
+        const float2 r = __ffma2_rn(make_float2(s, s), f2_of(v), f2_of(acc));
+        acc = cplx<T>{r.x, r.y};
+        return;
+    }
+#endif
     acc.re += s * v.re;
     acc.im += s * v.im;
 }
 // a + b
-template <typename T>
-__device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b) { return a + b; }
-// s * v (s real)
-template <typename T>
-__device__ __forceinline__ cplx<T> cscale(T s, cplx<T> v) { return s * v; }
+template <bool PK = false, typename T>
+__device__ __forceinline__ cplx<T> cadd(cplx<T> a, cplx<T> b)
+{
 #if H3D_F32X2
-__device__ __forceinline__ float2 f2_of(cplx<float> a) { return make_float2(a.re, a.im); }
-template <>
-__device__ __forceinline__ void fma_rc<float>(cplx<float> &acc, float s, cplx<float> v)
-{
-    const float2 r = __ffma2_rn(make_float2(s, s), f2_of(v), f2_of(acc));
-    acc = cplx<float>{r.x, r.y};
-}
-template <>
-__device__ __forceinline__ cplx<float> cadd<float>(cplx<float> a, cplx<float> b)
-{
-    const float2 r = __fadd2_rn(f2_of(a), f2_of(b));
-    return cplx<float>{r.x, r.y};
-}
-template <>
-__device__ __forceinline__ cplx<float> cscale<float>(float s, cplx<float> v)
-{
-    const float2 r = __fmul2_rn(make_float2(s, s), f2_of(v));
-    return cplx<float>{r.x, r.y};
-}
+    if constexpr (PK && sizeof(T) == 4) {
+        const float2 r = __fadd2_rn(f2_of(a), f2_of(b));
+        return cplx<T>{r.x, r.y};
+    }
 #endif
+    return a + b;
+}
+// s * v (s real)
+template <bool PK = false, typename T>
+__device__ __forceinline__ cplx<T> cscale(T s, cplx<T> v)
+{
+#if H3D_F32X2
+    if constexpr (PK && sizeof(T) == 4) {
+        const float2 r = __fmul2_rn(make_float2(s, s), f2_of(v));
+        return cplx<T>{r.x, r.y};
+    }
+#endif
+    return s * v;
+}
 
 // A running sum of complex products.  Complex128: one accumulator, chained FMAs (cmac).
-// Complex64: the two packed partial sums described above.
+// Complex64: two partial sums P += a.re * b and Q += a.im * b (two independent FMA chains,
+// or one packed instruction each), the product sum being (P.re - Q.im, P.im + Q.re).
 template <typename T>
 struct CSum {
     cplx<T> p, q;
 };
 template <typename T>
 __device__ __forceinline__ CSum<T> csum_init(cplx<T> v0) { return CSum<T>{v0, mk<T>(T(0), T(0))}; }
-template <typename T>
+template <bool PK = false, typename T>
 __device__ __forceinline__ void csum_mac(CSum<T> &s, cplx<T> a, cplx<T> b)
 {
     if constexpr (sizeof(T) == 4) {
-        fma_rc(s.p, a.re, b);
-        fma_rc(s.q, a.im, b);
+        fma_rc<PK>(s.p, a.re, b);
+        fma_rc<PK>(s.q, a.im, b);
     } else {
         cmac(s.p, a, b);
     }
 }
 // s += conj(a) * b
-template <typename T>
+template <bool PK = false, typename T>
 __device__ __forceinline__ void csum_mac_ca(CSum<T> &s, cplx<T> a, cplx<T> b)
 {
     if constexpr (sizeof(T) == 4) {
-        fma_rc(s.p, a.re, b);
-        fma_rc(s.q, -a.im, b);
+        fma_rc<PK>(s.p, a.re, b);
+        fma_rc<PK>(s.q, -a.im, b);
     } else {
         cmac(s.p, cconj(a), b);
     }
@@ -139,8 +148,8 @@ __device__ __forceinline__ cplx<T> csum_value(const CSum<T> &s)
     if constexpr (sizeof(T) == 4) return mk<T>(s.p.re - s.q.im, s.p.im + s.q.re);
     else return s.p;
 }
-// acc += d * conj(c), the Kaczmarz scatter: c.re (d.re, d.im) + c.im (d.im, -d.re), two
-// packed FMAs with the pairs (d.re, d.im) and (d.im, -d.re) formed once per row
+// acc += d * conj(c), the Kaczmarz scatter: c.re (d.re, d.im) + c.im (d.im, -d.re), with the
+// pairs (d.re, d.im) and (d.im, -d.re) formed once per row
 template <typename T>
 struct Scat {
     cplx<T> d1, d2;

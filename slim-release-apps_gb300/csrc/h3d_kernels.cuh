@@ -22,6 +22,9 @@ __device__ __forceinline__ cplx<float> load_cg(const cplx<float> *p)
 }
 
 // h3d_mvp.cu: z-marching matvec, and the FP64 residual b - A x with per-block norms.
+// mvp_prime_occupancy: fixes the device occupancy the matvec grids are cut by (called when
+// an operator is made).
+void mvp_prime_occupancy();
 int mvp_residual_parts(const Op<double> &op, int nrhs);
 int launch_residual(const Op<double> &op, const cplx<double> *b, const cplx<double> *x, cplx<double> *r,
                     int nrhs, bool adj, double *part, cudaStream_t st);

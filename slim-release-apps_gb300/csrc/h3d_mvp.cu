@@ -184,14 +184,69 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
     }
 }
 
-static int chunk_len(int nz) { return nz < 32 ? nz : 16; }
+// CTAs of the z-march kernel resident on the whole device (occupancy of the forward
+// variant of the precision and mode), queried once per device and kept for the process:
+// the residual's partial-sum buffer is sized from the same grid as the launch, so the
+// answer never changes (a failed query is remembered as "unknown").  make_op primes it,
+// outside any stream capture.
+template <typename T, bool RESID>
+static int zmarch_slots()
+{
+    static int cache[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return 0;
+    }
+    if (cache[dev] == 0) {
+        int per_sm = 0, sms = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mvp_zmarch_kernel<T, false, false, false, RESID>,
+                                                          kMX * kMY, 0) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+            cudaGetLastError();
+            per_sm = 0;
+        }
+        cache[dev] = per_sm * sms > 0 ? per_sm * sms : -1;
+    }
+    return cache[dev] > 0 ? cache[dev] : 0;
+}
 
-template <typename T>
+void mvp_prime_occupancy()
+{
+    zmarch_slots<float, false>();
+    zmarch_slots<double, false>();
+    zmarch_slots<float, true>();
+    zmarch_slots<double, true>();
+}
+
+// Split of the z axis into marching chunks.  A CTA's time grows with the planes it marches
+// (its rows plus the two halo planes), and the launch takes as many rounds of resident CTAs
+// as the grid needs: the split minimises rounds x (chunk + 2), which balances the halo
+// overhead of short chunks against the partly empty last round of a grid that does not fill
+// the device (config 1, 201 x 201 x 101: 5 chunks of 21 planes, 910 CTAs in 3 full rounds
+// of 304).  Without an occupancy figure, chunks of 16 planes.
+template <typename T, bool RESID>
 static dim3 zmarch_grid(const Op<T> &op, int nrhs, int *kz, int *nchunks)
 {
-    *kz = chunk_len(op.nz);
+    const long long gx = (op.nx + kMX - 1) / kMX, gy = (op.ny + kMY - 1) / kMY;
+    const int slots = zmarch_slots<T, RESID>();
+    int best_kz = op.nz < 32 ? op.nz : 16;
+    if (slots > 0) {
+        long long best = -1;
+        const int nmax = op.nz < 64 ? op.nz : 64;
+        for (int n = 1; n <= nmax; ++n) {
+            const int k = (op.nz + n - 1) / n;
+            const long long ctas = gx * gy * (long long)((op.nz + k - 1) / k) * nrhs;
+            const long long cost = ((ctas + slots - 1) / slots) * (k + 2);
+            if (best < 0 || cost < best) {
+                best = cost;
+                best_kz = k;
+            }
+        }
+    }
+    *kz = best_kz;
     *nchunks = (op.nz + *kz - 1) / *kz;
-    return dim3((op.nx + kMX - 1) / kMX, (op.ny + kMY - 1) / kMY, *nchunks * nrhs);
+    return dim3((unsigned)gx, (unsigned)gy, *nchunks * nrhs);
 }
 
 template <typename T, bool RESID>
@@ -199,7 +254,7 @@ static int zmarch_dispatch(const Op<T> &op, const cplx<T> *x, cplx<T> *y, const 
                            bool adj, bool deriv, double *part, cudaStream_t st)
 {
     int kz, nch;
-    const dim3 grd = zmarch_grid(op, nrhs, &kz, &nch);
+    const dim3 grd = zmarch_grid<T, RESID>(op, nrhs, &kz, &nch);
     if ((long long)nch * nrhs > 65535) {
         set_error("too many right-hand sides for one launch");
         return H3D_ERR_BAD_ARG;
@@ -230,7 +285,7 @@ int launch_mvp(const Op<T> &op, const cplx<T> *x, cplx<T> *y, int nrhs, bool adj
 int mvp_residual_parts(const Op<double> &op, int nrhs)
 {
     int kz, nch;
-    const dim3 g = zmarch_grid(op, nrhs, &kz, &nch);
+    const dim3 g = zmarch_grid<double, true>(op, nrhs, &kz, &nch);
     return (int)(g.x * g.y * nch);
 }
 

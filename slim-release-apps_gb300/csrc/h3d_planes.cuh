@@ -22,7 +22,7 @@ template <typename T, bool WNC>
 __device__ __forceinline__ cplx<T> wmul(cplx<T> w, cplx<T> v)
 {
     if constexpr (WNC) return w * v;
-    else return cscale(w.re, v);
+    else return cscale<true>(w.re, v);
 }
 
 template <typename T, bool ADJ, bool WNC, int PITCH>
@@ -41,10 +41,10 @@ __device__ __forceinline__ PlaneSums<T> plane_sums(const cplx<T> *sxp, const T *
     p.fxp = X(1, 0);
     p.fym = X(0, -1);
     p.fyp = X(0, 1);
-    p.cxm = cadd(mm, mp);
-    p.cxp = cadd(pm, pp);
-    p.cym = cadd(mm, pm);
-    p.cyp = cadd(mp, pp);
+    p.cxm = cadd<true>(mm, mp);
+    p.cxp = cadd<true>(pm, pp);
+    p.cym = cadd<true>(mm, pm);
+    p.cyp = cadd<true>(mp, pp);
     if constexpr (!ADJ) {
         p.wm = wmul<T, WNC>(W(0, 0), p.m);
         if constexpr (WNC) {
@@ -54,20 +54,20 @@ __device__ __forceinline__ PlaneSums<T> plane_sums(const cplx<T> *sxp, const T *
                     wmul<T, WNC>(W(1, 1), pp);
         } else {
             // real wavenumber: products then accumulated one FMA each
-            p.wfx = cscale(W(-1, 0).re, p.fxm);
-            fma_rc(p.wfx, W(1, 0).re, p.fxp);
-            p.wfy = cscale(W(0, -1).re, p.fym);
-            fma_rc(p.wfy, W(0, 1).re, p.fyp);
-            p.wc4 = cscale(W(-1, -1).re, mm);
-            fma_rc(p.wc4, W(-1, 1).re, mp);
-            fma_rc(p.wc4, W(1, -1).re, pm);
-            fma_rc(p.wc4, W(1, 1).re, pp);
+            p.wfx = cscale<true>(W(-1, 0).re, p.fxm);
+            fma_rc<true>(p.wfx, W(1, 0).re, p.fxp);
+            p.wfy = cscale<true>(W(0, -1).re, p.fym);
+            fma_rc<true>(p.wfy, W(0, 1).re, p.fyp);
+            p.wc4 = cscale<true>(W(-1, -1).re, mm);
+            fma_rc<true>(p.wc4, W(-1, 1).re, mp);
+            fma_rc<true>(p.wc4, W(1, -1).re, pm);
+            fma_rc<true>(p.wc4, W(1, 1).re, pp);
         }
     } else {
         p.wm = p.m;
-        p.wfx = cadd(p.fxm, p.fxp);
-        p.wfy = cadd(p.fym, p.fyp);
-        p.wc4 = cadd(p.cxm, p.cxp);
+        p.wfx = cadd<true>(p.fxm, p.fxp);
+        p.wfy = cadd<true>(p.fym, p.fyp);
+        p.wc4 = cadd<true>(p.cxm, p.cxp);
     }
     return p;
 }
@@ -96,33 +96,33 @@ __device__ __forceinline__ void acc_plane(RowAcc<T> &a, const PlaneSums<T> &P, c
 {
     const T w3 = op.w3a2;
     if constexpr (ROLE == 1) {
-        fma_rc(a.mass, op.wn_c, P.wm);
-        fma_rc(a.mass, T(-kWM2), cadd(P.wfx, P.wfy));
-        fma_rc(a.mass, T(-kWM3), P.wc4);
+        fma_rc<true>(a.mass, op.wn_c, P.wm);
+        fma_rc<true>(a.mass, T(-kWM2), cadd<true>(P.wfx, P.wfy));
+        fma_rc<true>(a.mass, T(-kWM3), P.wc4);
     } else {
-        fma_rc(a.mass, T(-kWM2), P.wm);
-        fma_rc(a.mass, T(-kWM3), cadd(P.wfx, P.wfy));
-        fma_rc(a.mass, T(-kWM4), P.wc4);
+        fma_rc<true>(a.mass, T(-kWM2), P.wm);
+        fma_rc<true>(a.mass, T(-kWM3), cadd<true>(P.wfx, P.wfy));
+        fma_rc<true>(a.mass, T(-kWM4), P.wc4);
     }
     if constexpr (!DERIV) {
-        const cplx<T> fx = cadd(P.fxm, P.fxp), fy = cadd(P.fym, P.fyp), c4 = cadd(P.cxm, P.cxp);
+        const cplx<T> fx = cadd<true>(P.fxm, P.fxp), fy = cadd<true>(P.fym, P.fyp), c4 = cadd<true>(P.cxm, P.cxp);
         if constexpr (ROLE == 1) {
-            fma_rc(a.bxm, op.pml_x, P.fxm); fma_rc(a.bxm, -op.xy, P.cxm);
-            fma_rc(a.bxp, op.pml_x, P.fxp); fma_rc(a.bxp, -op.xy, P.cxp);
-            fma_rc(a.bym, op.pml_y, P.fym); fma_rc(a.bym, -op.xy, P.cym);
-            fma_rc(a.byp, op.pml_y, P.fyp); fma_rc(a.byp, -op.xy, P.cyp);
-            fma_rc(a.bsx, op.wn_x, P.m); fma_rc(a.bsx, op.xy, fy);
-            fma_rc(a.bsy, op.wn_y, P.m); fma_rc(a.bsy, op.xy, fx);
-            fma_rc(a.bsz, op.wn_z, P.m); fma_rc(a.bsz, op.xz, fx); fma_rc(a.bsz, op.yz, fy); fma_rc(a.bsz, w3, c4);
+            fma_rc<true>(a.bxm, op.pml_x, P.fxm); fma_rc<true>(a.bxm, -op.xy, P.cxm);
+            fma_rc<true>(a.bxp, op.pml_x, P.fxp); fma_rc<true>(a.bxp, -op.xy, P.cxp);
+            fma_rc<true>(a.bym, op.pml_y, P.fym); fma_rc<true>(a.bym, -op.xy, P.cym);
+            fma_rc<true>(a.byp, op.pml_y, P.fyp); fma_rc<true>(a.byp, -op.xy, P.cyp);
+            fma_rc<true>(a.bsx, op.wn_x, P.m); fma_rc<true>(a.bsx, op.xy, fy);
+            fma_rc<true>(a.bsy, op.wn_y, P.m); fma_rc<true>(a.bsy, op.xy, fx);
+            fma_rc<true>(a.bsz, op.wn_z, P.m); fma_rc<true>(a.bsz, op.xz, fx); fma_rc<true>(a.bsz, op.yz, fy); fma_rc<true>(a.bsz, w3, c4);
         } else {
-            fma_rc(a.bxm, -op.xz, P.fxm); fma_rc(a.bxm, -w3, P.cxm);
-            fma_rc(a.bxp, -op.xz, P.fxp); fma_rc(a.bxp, -w3, P.cxp);
-            fma_rc(a.bym, -op.yz, P.fym); fma_rc(a.bym, -w3, P.cym);
-            fma_rc(a.byp, -op.yz, P.fyp); fma_rc(a.byp, -w3, P.cyp);
-            fma_rc(a.bsx, op.xz, P.m); fma_rc(a.bsx, w3, fy);
-            fma_rc(a.bsy, op.yz, P.m); fma_rc(a.bsy, w3, fx);
+            fma_rc<true>(a.bxm, -op.xz, P.fxm); fma_rc<true>(a.bxm, -w3, P.cxm);
+            fma_rc<true>(a.bxp, -op.xz, P.fxp); fma_rc<true>(a.bxp, -w3, P.cxp);
+            fma_rc<true>(a.bym, -op.yz, P.fym); fma_rc<true>(a.bym, -w3, P.cym);
+            fma_rc<true>(a.byp, -op.yz, P.fyp); fma_rc<true>(a.byp, -w3, P.cyp);
+            fma_rc<true>(a.bsx, op.xz, P.m); fma_rc<true>(a.bsx, w3, fy);
+            fma_rc<true>(a.bsy, op.yz, P.m); fma_rc<true>(a.bsy, w3, fx);
             cplx<T> &bz = ROLE == 0 ? a.bzm : a.bzp;
-            fma_rc(bz, op.pml_z, P.m); fma_rc(bz, -op.xz, fx); fma_rc(bz, -op.yz, fy); fma_rc(bz, -w3, c4);
+            fma_rc<true>(bz, op.pml_z, P.m); fma_rc<true>(bz, -op.xz, fx); fma_rc<true>(bz, -op.yz, fy); fma_rc<true>(bz, -w3, c4);
         }
     }
 }
@@ -133,12 +133,12 @@ template <typename T, bool ADJ, bool DERIV, bool WNC>
 __device__ __forceinline__ cplx<T> acc_finish(const RowAcc<T> &a, const RowPml<T> &p, cplx<T> wc)
 {
     cplx<T> y = a.mass;
-    if constexpr (ADJ) y = WNC ? cconj(wc) * y : cscale(wc.re, y);
+    if constexpr (ADJ) y = WNC ? cconj(wc) * y : cscale<true>(wc.re, y);
     if constexpr (!DERIV) {
         CSum<T> s = csum_init(y);
         auto mac = [&](cplx<T> f, cplx<T> br) {
-            if constexpr (ADJ) csum_mac_ca(s, f, br);
-            else csum_mac(s, f, br);
+            if constexpr (ADJ) csum_mac_ca<true>(s, f, br);
+            else csum_mac<true>(s, f, br);
         };
         mac(p.Axm, a.bxm);
         mac(p.Axp, a.bxp);
@@ -162,31 +162,31 @@ template <int ROLE, typename T, bool ZI>
 __device__ __forceinline__ void acc_plane_xy(RowAcc<T> &a, const PlaneSums<T> &P, const Op<T> &op)
 {
     if constexpr (ROLE == 1) {
-        fma_rc(a.mass, op.wn_c, P.wm);
-        fma_rc(a.mass, T(-kWM2), cadd(P.wfx, P.wfy));
-        fma_rc(a.mass, T(-kWM3), P.wc4);
+        fma_rc<true>(a.mass, op.wn_c, P.wm);
+        fma_rc<true>(a.mass, T(-kWM2), cadd<true>(P.wfx, P.wfy));
+        fma_rc<true>(a.mass, T(-kWM3), P.wc4);
     } else {
-        fma_rc(a.mass, T(-kWM2), P.wm);
-        fma_rc(a.mass, T(-kWM3), cadd(P.wfx, P.wfy));
-        fma_rc(a.mass, T(-kWM4), P.wc4);
+        fma_rc<true>(a.mass, T(-kWM2), P.wm);
+        fma_rc<true>(a.mass, T(-kWM3), cadd<true>(P.wfx, P.wfy));
+        fma_rc<true>(a.mass, T(-kWM4), P.wc4);
     }
-    const cplx<T> fx = cadd(P.fxm, P.fxp), fy = cadd(P.fym, P.fyp), c4 = cadd(P.cxm, P.cxp);
+    const cplx<T> fx = cadd<true>(P.fxm, P.fxp), fy = cadd<true>(P.fym, P.fyp), c4 = cadd<true>(P.cxm, P.cxp);
     cplx<T> &r = a.bsx;
     if constexpr (ZI) {
         if constexpr (ROLE == 1) {
-            fma_rc(r, op.kint[1], fx); fma_rc(r, op.kint[2], fy); fma_rc(r, op.kint[4], c4); fma_rc(r, op.kint[0], P.m);
+            fma_rc<true>(r, op.kint[1], fx); fma_rc<true>(r, op.kint[2], fy); fma_rc<true>(r, op.kint[4], c4); fma_rc<true>(r, op.kint[0], P.m);
         } else {
-            fma_rc(r, op.kint[5], fx); fma_rc(r, op.kint[6], fy); fma_rc(r, op.kint[7], c4); fma_rc(r, op.kint[3], P.m);
+            fma_rc<true>(r, op.kint[5], fx); fma_rc<true>(r, op.kint[6], fy); fma_rc<true>(r, op.kint[7], c4); fma_rc<true>(r, op.kint[3], P.m);
         }
     } else {
         const T w3 = op.w3a2;
         if constexpr (ROLE == 1) {
-            fma_rc(r, op.kxy[0], fx); fma_rc(r, op.kxy[1], fy); fma_rc(r, op.kxy[2], c4); fma_rc(r, op.kxy[3], P.m);
-            fma_rc(a.bsz, op.wn_z, P.m); fma_rc(a.bsz, op.xz, fx); fma_rc(a.bsz, op.yz, fy); fma_rc(a.bsz, w3, c4);
+            fma_rc<true>(r, op.kxy[0], fx); fma_rc<true>(r, op.kxy[1], fy); fma_rc<true>(r, op.kxy[2], c4); fma_rc<true>(r, op.kxy[3], P.m);
+            fma_rc<true>(a.bsz, op.wn_z, P.m); fma_rc<true>(a.bsz, op.xz, fx); fma_rc<true>(a.bsz, op.yz, fy); fma_rc<true>(a.bsz, w3, c4);
         } else {
-            fma_rc(r, op.kxy[4], fx); fma_rc(r, op.kxy[5], fy); fma_rc(r, op.kxy[6], c4); fma_rc(r, op.kxy[7], P.m);
+            fma_rc<true>(r, op.kxy[4], fx); fma_rc<true>(r, op.kxy[5], fy); fma_rc<true>(r, op.kxy[6], c4); fma_rc<true>(r, op.kxy[7], P.m);
             cplx<T> &bz = ROLE == 0 ? a.bzm : a.bzp;
-            fma_rc(bz, op.pml_z, P.m); fma_rc(bz, -op.xz, fx); fma_rc(bz, -op.yz, fy); fma_rc(bz, -w3, c4);
+            fma_rc<true>(bz, op.pml_z, P.m); fma_rc<true>(bz, -op.xz, fx); fma_rc<true>(bz, -op.yz, fy); fma_rc<true>(bz, -w3, c4);
         }
     }
 }
@@ -196,13 +196,13 @@ template <typename T, bool ADJ, bool ZI>
 __device__ __forceinline__ cplx<T> acc_finish_xy(const RowAcc<T> &a, const RowPml<T> &p, cplx<T> wc)
 {
     cplx<T> y = a.mass;
-    if constexpr (ADJ) y = cscale(wc.re, y);
-    y = cadd(y, a.bsx);
+    if constexpr (ADJ) y = cscale<true>(wc.re, y);
+    y = cadd<true>(y, a.bsx);
     if constexpr (!ZI) {
         CSum<T> s = csum_init(y);
         auto mac = [&](cplx<T> f, cplx<T> br) {
-            if constexpr (ADJ) csum_mac_ca(s, f, br);
-            else csum_mac(s, f, br);
+            if constexpr (ADJ) csum_mac_ca<true>(s, f, br);
+            else csum_mac<true>(s, f, br);
         };
         mac(p.Azm, a.bzm);
         mac(p.Azp, a.bzp);
