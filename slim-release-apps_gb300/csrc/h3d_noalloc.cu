@@ -54,13 +54,15 @@ extern "C" int h3d_residual_noalloc(const h3d_grid *g, const double *wn_re, cons
                                     const void *b, const void *x, void *r, double *rr2, double *bb2,
                                     int nrhs, int mode, void *stream)
 {
-    if (!wn_re || !b || !x || !r || nrhs < 1 || (mode != H3D_FORWARD && mode != H3D_ADJOINT)) {
+    if (nrhs < 1 || (mode != H3D_FORWARD && mode != H3D_ADJOINT)) {
         set_error("h3d_residual_noalloc: bad argument");
         return H3D_ERR_BAD_ARG;
     }
     int rc = check_grid(g);
     if (rc) return rc;
-    // Size check first, before any device call.
+    // Size check first, before any device call and before the pointers are looked at: a
+    // call with the data pointers left NULL asks only whether the problem fits the scratch,
+    // and can never launch.
     size_t tab_entries = 0;
     for (int a = 0; a < 3; ++a) tab_entries += 3 * (size_t)(g->n[a] + 2);
     const size_t tab_doubles = (2 * tab_entries + 31) / 32 * 32;  // keep the partials 256-byte aligned
@@ -74,6 +76,10 @@ extern "C" int h3d_residual_noalloc(const h3d_grid *g, const double *wn_re, cons
         set_error("h3d_residual_noalloc: grid %dx%dx%d with %d right-hand sides needs %zu bytes of scratch, "
                   "more than the fixed %u bytes",
                   g->n[0], g->n[1], g->n[2], nrhs, need * sizeof(double), (unsigned)H3D_NOALLOC_SCRATCH_BYTES);
+        return H3D_ERR_BAD_ARG;
+    }
+    if (!wn_re || !b || !x || !r) {
+        set_error("h3d_residual_noalloc: bad argument");
         return H3D_ERR_BAD_ARG;
     }
     double *scratch = nullptr;

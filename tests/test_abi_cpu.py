@@ -89,3 +89,20 @@ def test_sinc_weights_host_match_oracle():
                 if 0 <= idx < n:
                     mine[idx] = w[p, a, o]
             np.testing.assert_allclose(mine, full, rtol=0, atol=1e-14)
+
+
+def test_noalloc_residual_size_check_is_host_only():
+    """h3d_residual_noalloc refuses a problem beyond its fixed scratch before any device
+    call and before it looks at the data pointers (left NULL here)."""
+    from h3d import _lib as L
+
+    lib = L.load()
+    grid = L.make_grid((400, 400, 400), (10.0, 10.0, 10.0), 10)
+    rc = lib.h3d_residual_noalloc(C.byref(grid), None, None, None, None, None, None, None, 4096, L.FORWARD, None)
+    assert rc == L.ERR_BAD_ARG
+    assert b"scratch" in lib.h3d_last_error()
+    # a problem that fits is refused by the pointer check instead, still without device work
+    small = L.make_grid((16, 16, 16), (10.0, 10.0, 10.0), 2)
+    rc = lib.h3d_residual_noalloc(C.byref(small), None, None, None, None, None, None, None, 1, L.FORWARD, None)
+    assert rc == L.ERR_BAD_ARG
+    assert b"scratch" not in lib.h3d_last_error()

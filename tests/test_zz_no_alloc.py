@@ -56,12 +56,14 @@ def test_noalloc_residual_rejects_problems_beyond_its_scratch(cuda):
     from h3d import _lib as L
 
     lib = L.load()
-    n = (400, 400, 400)            # needs far more partial sums than the fixed scratch holds
+    # 400^3 with 4096 right-hand sides needs at least 2 x 650 x 4096 partial sums (one column
+    # block per 32 x 8 columns, whatever the z split), far more than the fixed scratch.  The
+    # data pointers stay NULL: the size check runs first, and a call that passed it would be
+    # refused by the pointer check instead, so this test can never launch a kernel.
+    n = (400, 400, 400)
     grid = L.make_grid(n, (10.0, 10.0, 10.0), 10)
-    dummy = torch.zeros(8, dtype=torch.complex128, device=cuda)
-    rc = lib.h3d_residual_noalloc(C.byref(grid), C.c_void_p(dummy.data_ptr()), C.c_void_p(),
-                                  C.c_void_p(dummy.data_ptr()), C.c_void_p(dummy.data_ptr()),
-                                  C.c_void_p(dummy.data_ptr()), C.c_void_p(), C.c_void_p(), 64,
+    rc = lib.h3d_residual_noalloc(C.byref(grid), C.c_void_p(), C.c_void_p(), C.c_void_p(), C.c_void_p(),
+                                  C.c_void_p(), C.c_void_p(), C.c_void_p(), 4096,
                                   L.FORWARD, C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == L.ERR_BAD_ARG
     assert b"scratch" in lib.h3d_last_error()
