@@ -57,10 +57,13 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
     const cplx<T> *xs = x + (long long)s * op.N;
 
     // Staging: the CTA's halo'd plane has kPN points; thread tid copies points tid and
-    // tid + kMX*kMY.  Their in-plane offsets and x/y bounds are fixed for the march.
+    // tid + kMX*kMY.  Their in-plane offsets (32-bit: the host refuses nx*ny >= 2^31) and
+    // x/y bounds are fixed for the march; per plane only the plane's base pointers change
+    // (the same for every thread).  Points outside the grid copy nothing (zero fill) from a
+    // valid address: the plane base, or plane 0 for planes outside the grid.
     constexpr int kNT = kMX * kMY;
     constexpr int kSlots = (kPN + kNT - 1) / kNT;
-    long long goff[kSlots];
+    int goff[kSlots];
     bool gin[kSlots];
 #pragma unroll
     for (int q = 0; q < kSlots; ++q) {
@@ -68,21 +71,24 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
         const int li = e % kPX, lj = e / kPX;
         const int gi = i0 - 1 + li, gj = j0 - 1 + lj;
         gin[q] = e < kPN && gi >= 0 && gi < op.nx && gj >= 0 && gj < op.ny;
-        goff[q] = gin[q] ? gi + op.sy * gj : 0;
+        goff[q] = gin[q] ? gi + op.nx * gj : 0;
     }
     auto stage = [&](int buf, int pk) {
         const bool kin = pk >= 0 && pk < op.nz;
         const long long zo = kin ? op.sz * pk : 0;
+        const cplx<T> *xp = xs + zo;
+        const T *wp = op.wn + zo;
+        const T *wip = WNC ? op.wni + zo : nullptr;
 #pragma unroll
         for (int q = 0; q < kSlots; ++q) {
             const int e = tid + q * kNT;
             if (e < kPN) {
                 const bool in = kin && gin[q];
-                const long long g = in ? goff[q] + zo : 0;
-                mv_cp_async<sizeof(cplx<T>)>(&sx[buf][e], xs + g, in);
+                const int g = in ? goff[q] : 0;
+                mv_cp_async<sizeof(cplx<T>)>(&sx[buf][e], xp + g, in);
                 if constexpr (NEED_WN) {
-                    mv_cp_async<sizeof(T)>(&swr[buf][e], op.wn + g, in);
-                    if constexpr (WNC) mv_cp_async<sizeof(T)>(&swi[buf][e], op.wni + g, in);
+                    mv_cp_async<sizeof(T)>(&swr[buf][e], wp + g, in);
+                    if constexpr (WNC) mv_cp_async<sizeof(T)>(&swi[buf][e], wip + g, in);
                 }
             }
         }
@@ -98,11 +104,13 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
                        j0 + kMY <= ihi[1];
     auto zint = [&](int k) { return k >= ilo[2] && k < ihi[2]; };
     const int l = (threadIdx.x + 1) + kPX * (threadIdx.y + 1);
+    const long long col = i + op.sy * j;  // the thread's column: row k at col + k sz
     double rr = 0.0, bb = 0.0;
 
-    // One plane pk: add it to the pending rows pk-1 (lo), pk (mid) and pk+1 (hi), finish
-    // row pk-1 and clear its accumulator, which then serves row pk+2.  The caller rotates
-    // the three accumulators' roles, so no accumulator is ever copied.
+    // One plane pk: add it to the pending rows pk-1 (lo), pk (mid) and pk+1 (hi) and finish
+    // row pk-1, whose accumulator then serves row pk+2 (its first plane sets every bracket,
+    // so nothing is cleared).  The caller rotates the three accumulators' roles, so no
+    // accumulator is ever copied.
     auto step = [&](int pk, RowAcc<T> &lo, RowAcc<T> &mid, RowAcc<T> &hi) {
         const int buf = (pk - (kb - 1)) & 1;
         if (pk + 1 <= ke) {
@@ -144,7 +152,7 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
                     p.Azp = t[op.lo[2] + k + 2];
                 }
             }
-            const long long ctr = i + op.sy * j + op.sz * k;
+            const long long ctr = col + op.sz * k;
             cplx<T> wc = mk<T>(T(0), T(0));
             if constexpr (ADJ) wc = load_wn<T, WNC>(op, ctr);
             const cplx<T> v = !xyint     ? acc_finish<T, ADJ, DERIV, WNC>(lo, p, wc)
@@ -160,7 +168,6 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
                 y[(long long)s * op.N + ctr] = v;
             }
         }
-        acc_zero(lo);
     };
 
     RowAcc<T> Q0, Q1, Q2;  // rows pk-1, pk, pk+1 at the top of the loop
@@ -253,6 +260,10 @@ template <typename T, bool RESID>
 static int zmarch_dispatch(const Op<T> &op, const cplx<T> *x, cplx<T> *y, const cplx<T> *b, int nrhs,
                            bool adj, bool deriv, double *part, cudaStream_t st)
 {
+    if ((long long)op.nx * op.ny >= (1LL << 31)) {
+        set_error("a z plane of more than 2^31 - 1 points is not supported by the matvec");
+        return H3D_ERR_NSIZE;
+    }
     int kz, nch;
     const dim3 grd = zmarch_grid<T, RESID>(op, nrhs, &kz, &nch);
     if ((long long)nch * nrhs > 65535) {

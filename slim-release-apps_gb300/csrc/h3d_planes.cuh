@@ -90,17 +90,29 @@ __device__ __forceinline__ void acc_zero(RowAcc<T> &a)
     a.mass = a.bxm = a.bxp = a.bym = a.byp = a.bzm = a.bzp = a.bsx = a.bsy = a.bsz = z;
 }
 
+// acc = s v (SET: the bracket's first term for this row) or acc += s v.  Every bracket is
+// set by the first plane that touches it -- role 0 for all but bsz (role 1) and bzp
+// (role 2) -- so a finished row's accumulators need no clearing before they serve the next
+// row.  s v equals 0 + s v exactly, so the values do not change.
+template <bool SET, typename T>
+__device__ __forceinline__ void put_rc(cplx<T> &acc, T s, cplx<T> v)
+{
+    if constexpr (SET) acc = cscale<true>(s, v);
+    else fma_rc<true>(acc, s, v);
+}
+
 // ROLE: 0 = the plane below the row (k-1), 1 = the row's plane, 2 = the plane above.
 template <int ROLE, typename T, bool DERIV>
 __device__ __forceinline__ void acc_plane(RowAcc<T> &a, const PlaneSums<T> &P, const Op<T> &op)
 {
+    constexpr bool F = ROLE == 0;  // first plane of the row
     const T w3 = op.w3a2;
     if constexpr (ROLE == 1) {
         fma_rc<true>(a.mass, op.wn_c, P.wm);
         fma_rc<true>(a.mass, T(-kWM2), cadd<true>(P.wfx, P.wfy));
         fma_rc<true>(a.mass, T(-kWM3), P.wc4);
     } else {
-        fma_rc<true>(a.mass, T(-kWM2), P.wm);
+        put_rc<F>(a.mass, T(-kWM2), P.wm);
         fma_rc<true>(a.mass, T(-kWM3), cadd<true>(P.wfx, P.wfy));
         fma_rc<true>(a.mass, T(-kWM4), P.wc4);
     }
@@ -113,16 +125,16 @@ __device__ __forceinline__ void acc_plane(RowAcc<T> &a, const PlaneSums<T> &P, c
             fma_rc<true>(a.byp, op.pml_y, P.fyp); fma_rc<true>(a.byp, -op.xy, P.cyp);
             fma_rc<true>(a.bsx, op.wn_x, P.m); fma_rc<true>(a.bsx, op.xy, fy);
             fma_rc<true>(a.bsy, op.wn_y, P.m); fma_rc<true>(a.bsy, op.xy, fx);
-            fma_rc<true>(a.bsz, op.wn_z, P.m); fma_rc<true>(a.bsz, op.xz, fx); fma_rc<true>(a.bsz, op.yz, fy); fma_rc<true>(a.bsz, w3, c4);
+            put_rc<true>(a.bsz, op.wn_z, P.m); fma_rc<true>(a.bsz, op.xz, fx); fma_rc<true>(a.bsz, op.yz, fy); fma_rc<true>(a.bsz, w3, c4);
         } else {
-            fma_rc<true>(a.bxm, -op.xz, P.fxm); fma_rc<true>(a.bxm, -w3, P.cxm);
-            fma_rc<true>(a.bxp, -op.xz, P.fxp); fma_rc<true>(a.bxp, -w3, P.cxp);
-            fma_rc<true>(a.bym, -op.yz, P.fym); fma_rc<true>(a.bym, -w3, P.cym);
-            fma_rc<true>(a.byp, -op.yz, P.fyp); fma_rc<true>(a.byp, -w3, P.cyp);
-            fma_rc<true>(a.bsx, op.xz, P.m); fma_rc<true>(a.bsx, w3, fy);
-            fma_rc<true>(a.bsy, op.yz, P.m); fma_rc<true>(a.bsy, w3, fx);
+            put_rc<F>(a.bxm, -op.xz, P.fxm); fma_rc<true>(a.bxm, -w3, P.cxm);
+            put_rc<F>(a.bxp, -op.xz, P.fxp); fma_rc<true>(a.bxp, -w3, P.cxp);
+            put_rc<F>(a.bym, -op.yz, P.fym); fma_rc<true>(a.bym, -w3, P.cym);
+            put_rc<F>(a.byp, -op.yz, P.fyp); fma_rc<true>(a.byp, -w3, P.cyp);
+            put_rc<F>(a.bsx, op.xz, P.m); fma_rc<true>(a.bsx, w3, fy);
+            put_rc<F>(a.bsy, op.yz, P.m); fma_rc<true>(a.bsy, w3, fx);
             cplx<T> &bz = ROLE == 0 ? a.bzm : a.bzp;
-            fma_rc<true>(bz, op.pml_z, P.m); fma_rc<true>(bz, -op.xz, fx); fma_rc<true>(bz, -op.yz, fy); fma_rc<true>(bz, -w3, c4);
+            put_rc<true>(bz, op.pml_z, P.m); fma_rc<true>(bz, -op.xz, fx); fma_rc<true>(bz, -op.yz, fy); fma_rc<true>(bz, -w3, c4);
         }
     }
 }
@@ -161,12 +173,13 @@ __device__ __forceinline__ cplx<T> acc_finish(const RowAcc<T> &a, const RowPml<T
 template <int ROLE, typename T, bool ZI>
 __device__ __forceinline__ void acc_plane_xy(RowAcc<T> &a, const PlaneSums<T> &P, const Op<T> &op)
 {
+    constexpr bool F = ROLE == 0;  // first plane of the row
     if constexpr (ROLE == 1) {
         fma_rc<true>(a.mass, op.wn_c, P.wm);
         fma_rc<true>(a.mass, T(-kWM2), cadd<true>(P.wfx, P.wfy));
         fma_rc<true>(a.mass, T(-kWM3), P.wc4);
     } else {
-        fma_rc<true>(a.mass, T(-kWM2), P.wm);
+        put_rc<F>(a.mass, T(-kWM2), P.wm);
         fma_rc<true>(a.mass, T(-kWM3), cadd<true>(P.wfx, P.wfy));
         fma_rc<true>(a.mass, T(-kWM4), P.wc4);
     }
@@ -176,17 +189,17 @@ __device__ __forceinline__ void acc_plane_xy(RowAcc<T> &a, const PlaneSums<T> &P
         if constexpr (ROLE == 1) {
             fma_rc<true>(r, op.kint[1], fx); fma_rc<true>(r, op.kint[2], fy); fma_rc<true>(r, op.kint[4], c4); fma_rc<true>(r, op.kint[0], P.m);
         } else {
-            fma_rc<true>(r, op.kint[5], fx); fma_rc<true>(r, op.kint[6], fy); fma_rc<true>(r, op.kint[7], c4); fma_rc<true>(r, op.kint[3], P.m);
+            put_rc<F>(r, op.kint[5], fx); fma_rc<true>(r, op.kint[6], fy); fma_rc<true>(r, op.kint[7], c4); fma_rc<true>(r, op.kint[3], P.m);
         }
     } else {
         const T w3 = op.w3a2;
         if constexpr (ROLE == 1) {
             fma_rc<true>(r, op.kxy[0], fx); fma_rc<true>(r, op.kxy[1], fy); fma_rc<true>(r, op.kxy[2], c4); fma_rc<true>(r, op.kxy[3], P.m);
-            fma_rc<true>(a.bsz, op.wn_z, P.m); fma_rc<true>(a.bsz, op.xz, fx); fma_rc<true>(a.bsz, op.yz, fy); fma_rc<true>(a.bsz, w3, c4);
+            put_rc<true>(a.bsz, op.wn_z, P.m); fma_rc<true>(a.bsz, op.xz, fx); fma_rc<true>(a.bsz, op.yz, fy); fma_rc<true>(a.bsz, w3, c4);
         } else {
-            fma_rc<true>(r, op.kxy[4], fx); fma_rc<true>(r, op.kxy[5], fy); fma_rc<true>(r, op.kxy[6], c4); fma_rc<true>(r, op.kxy[7], P.m);
+            put_rc<F>(r, op.kxy[4], fx); fma_rc<true>(r, op.kxy[5], fy); fma_rc<true>(r, op.kxy[6], c4); fma_rc<true>(r, op.kxy[7], P.m);
             cplx<T> &bz = ROLE == 0 ? a.bzm : a.bzp;
-            fma_rc<true>(bz, op.pml_z, P.m); fma_rc<true>(bz, -op.xz, fx); fma_rc<true>(bz, -op.yz, fy); fma_rc<true>(bz, -w3, c4);
+            put_rc<true>(bz, op.pml_z, P.m); fma_rc<true>(bz, -op.xz, fx); fma_rc<true>(bz, -op.yz, fy); fma_rc<true>(bz, -w3, c4);
         }
     }
 }
