@@ -56,9 +56,9 @@ DEFAULT_ORDER = "block8"
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of the
 # complex64 config-1 solve (python -m h3d.profile --kernel cgmn --config 1 --dtype c64,
-# the capture summarised in profiles/; mean of the two captured 27-step launches);
+# the capture summarised in profiles/; mean over the 15 launches of one double sweep);
 # keyed by (order, tuned variant).
-TRAFFIC_PER_LAUNCH = {("block8", 0): 112.30e6}
+TRAFFIC_PER_LAUNCH = {("block8", 0): 112.6e6}
 
 
 def _sweep_kernel(order, variant):
