@@ -26,8 +26,10 @@ __device__ __forceinline__ cplx<float> load_cg(const cplx<float> *p)
 // an operator is made).
 void mvp_prime_occupancy();
 int mvp_residual_parts(const Op<double> &op, int nrhs);
+// parts: the partial-sum count per right-hand side the buffer was sized for
+// (mvp_residual_parts); a launch needing another count is refused.
 int launch_residual(const Op<double> &op, const cplx<double> *b, const cplx<double> *x, cplx<double> *r,
-                    int nrhs, bool adj, double *part, cudaStream_t st);
+                    int nrhs, bool adj, double *part, int parts, cudaStream_t st);
 
 // h3d_mvp.cu / h3d_stencil.cu
 template <typename T>

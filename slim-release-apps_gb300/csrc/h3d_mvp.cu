@@ -37,6 +37,14 @@ __device__ __forceinline__ void mv_cp_async(void *sdst, const void *gsrc, bool v
         asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(s), "l"(gsrc), "n"(BYTES), "r"(n) : "memory");
 }
 
+// Origin shift of the column tiling along one axis: with tiles of t columns starting at
+// -shift, a tile boundary falls on the first row whose forward PML values are all 1 (lo), so
+// the interior columns fill whole tiles and take the folded-bracket path.
+__host__ __device__ inline int tile_shift(int lo, int hi, int t)
+{
+    return (lo > 0 && lo < hi && lo % t != 0) ? t - lo % t : 0;
+}
+
 template <typename T, bool ADJ, bool DERIV, bool WNC, bool RESID>
 __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cplx<T> *__restrict__ x,
                                                               cplx<T> *__restrict__ y,
@@ -51,9 +59,10 @@ __global__ void __launch_bounds__(kMX *kMY) mvp_zmarch_kernel(Op<T> op, const cp
     const int tid = threadIdx.x + kMX * threadIdx.y;
     const int s = blockIdx.z / nchunks, chunk = blockIdx.z % nchunks;
     const int kb = chunk * kz, ke = min(op.nz, kb + kz);
-    const int i0 = blockIdx.x * kMX, j0 = blockIdx.y * kMY;
+    const int i0 = blockIdx.x * kMX - tile_shift(op.int_lo_f[0], op.int_hi_f[0], kMX);
+    const int j0 = blockIdx.y * kMY - tile_shift(op.int_lo_f[1], op.int_hi_f[1], kMY);
     const int i = i0 + threadIdx.x, j = j0 + threadIdx.y;
-    const bool valid = i < op.nx && j < op.ny;
+    const bool valid = i >= 0 && i < op.nx && j >= 0 && j < op.ny;
     const cplx<T> *xs = x + (long long)s * op.N;
 
     // Staging: the CTA's halo'd plane has kPN points; thread tid copies points tid and
@@ -235,7 +244,8 @@ void mvp_prime_occupancy()
 template <typename T, bool RESID>
 static dim3 zmarch_grid(const Op<T> &op, int nrhs, int *kz, int *nchunks)
 {
-    const long long gx = (op.nx + kMX - 1) / kMX, gy = (op.ny + kMY - 1) / kMY;
+    const long long gx = (op.nx + tile_shift(op.int_lo_f[0], op.int_hi_f[0], kMX) + kMX - 1) / kMX;
+    const long long gy = (op.ny + tile_shift(op.int_lo_f[1], op.int_hi_f[1], kMY) + kMY - 1) / kMY;
     const int slots = zmarch_slots<T, RESID>();
     int best_kz = op.nz < 32 ? op.nz : 16;
     if (slots > 0) {
@@ -258,7 +268,7 @@ static dim3 zmarch_grid(const Op<T> &op, int nrhs, int *kz, int *nchunks)
 
 template <typename T, bool RESID>
 static int zmarch_dispatch(const Op<T> &op, const cplx<T> *x, cplx<T> *y, const cplx<T> *b, int nrhs,
-                           bool adj, bool deriv, double *part, cudaStream_t st)
+                           bool adj, bool deriv, double *part, int parts, cudaStream_t st)
 {
     if ((long long)op.nx * op.ny >= (1LL << 31)) {
         set_error("a z plane of more than 2^31 - 1 points is not supported by the matvec");
@@ -268,6 +278,12 @@ static int zmarch_dispatch(const Op<T> &op, const cplx<T> *x, cplx<T> *y, const 
     const dim3 grd = zmarch_grid<T, RESID>(op, nrhs, &kz, &nch);
     if ((long long)nch * nrhs > 65535) {
         set_error("too many right-hand sides for one launch");
+        return H3D_ERR_BAD_ARG;
+    }
+    if (RESID && (long long)grd.x * grd.y * nch != parts) {
+        // the partial-sum buffer was sized for another grid: refuse rather than overrun it
+        set_error("residual: %lld column blocks per right-hand side, buffer sized for %d",
+                  (long long)grd.x * grd.y * nch, parts);
         return H3D_ERR_BAD_ARG;
     }
     const dim3 blk(kMX, kMY);
@@ -290,7 +306,7 @@ template <typename T>
 int launch_mvp(const Op<T> &op, const cplx<T> *x, cplx<T> *y, int nrhs, bool adj, bool deriv,
                cudaStream_t st)
 {
-    return zmarch_dispatch<T, false>(op, x, y, nullptr, nrhs, adj, deriv, nullptr, st);
+    return zmarch_dispatch<T, false>(op, x, y, nullptr, nrhs, adj, deriv, nullptr, 0, st);
 }
 
 int mvp_residual_parts(const Op<double> &op, int nrhs)
@@ -301,9 +317,9 @@ int mvp_residual_parts(const Op<double> &op, int nrhs)
 }
 
 int launch_residual(const Op<double> &op, const cplx<double> *b, const cplx<double> *x, cplx<double> *r,
-                    int nrhs, bool adj, double *part, cudaStream_t st)
+                    int nrhs, bool adj, double *part, int parts, cudaStream_t st)
 {
-    return zmarch_dispatch<double, true>(op, x, r, b, nrhs, adj, false, part, st);
+    return zmarch_dispatch<double, true>(op, x, r, b, nrhs, adj, false, part, parts, st);
 }
 
 template int launch_mvp<double>(const Op<double> &, const cplx<double> *, cplx<double> *, int, bool, bool, cudaStream_t);

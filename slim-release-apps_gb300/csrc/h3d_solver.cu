@@ -46,7 +46,7 @@ int residual_f64(const Op<double> &op, const cplx<double> *b, const cplx<double>
                  cplx<double> *r, double *rr2, double *bb2, int nrhs, bool adj, double *part,
                  int G, cudaStream_t st)
 {
-    int rc = launch_residual(op, b, x, r, nrhs, adj, part, st);
+    int rc = launch_residual(op, b, x, r, nrhs, adj, part, G, st);
     if (rc) return rc;
     residual_reduce<<<nrhs, 256, 0, st>>>(part, G, rr2, bb2);
     H3D_CUDA_TRY(cudaGetLastError());
