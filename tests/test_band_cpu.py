@@ -1,0 +1,73 @@
+"""The band-storage (mat_free = false) oracle pinned against the reference, on CPU.
+
+oracle/slim_band.py restates helmholtz_3d.m / create_pml.m (the 27 x N band matrix),
+Htransp.m, Hmvp_MT_mex.c and sweep_MT_mex.c.  Pins:
+  * the restated band matrix times a vector equals the compiled matrix-free reference
+    matvec (Helm3dmvp_forw_mex / Helm3dmvp_adj_mex) to rounding: the two reference paths
+    build the same operator;
+  * the restated band matvec and band sweep equal the compiled band gateways
+    Hmvp_MT_mex / sweep_MT_mex (the sweep bit for bit);
+  * the band sweep of helmholtz_3d's matrix equals the matrix-free Kaczmarz sweep.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import mexharness as M
+from oracle import slim_band as SB
+
+BAND_REF = ("Hmvp_MT_mex", "sweep_MT_mex", "Helm3dmvp_forw_mex", "Helm3dmvp_adj_mex", "Helm3d_kacz_sweep_mex")
+pytestmark = pytest.mark.skipif(
+    not all(os.path.exists(os.path.join(M.REF_DIR, n + ".so")) for n in BAND_REF),
+    reason="reference gateways not compiled here")
+
+
+def _problem(seed, n=(9, 8, 7), npml=((3, 2, 3), (3, 2, 3))):
+    rng = np.random.default_rng(seed)
+    h = np.array([10.0, 12.0, 11.0])
+    wn = (2 * np.pi * 5) ** 2 / (1500 + 500 * rng.random(n)) ** 2
+    return rng, wn, h, np.array(npml, float)
+
+
+def _rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+def test_band_matrix_equals_matrix_free_operator():
+    rng, wn, h, npml = _problem(1)
+    n = wn.shape
+    N = wn.size
+    H, idx = SB.helmholtz_3d_bands(wn, h, npml)
+    assert H.shape == (27, N)
+    x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    args = (wn.reshape(-1, order="F"), h, np.array(n, float), npml, x, 1.0)
+    assert _rel(SB.band_mvp(H, idx, x), M.load_reference("Helm3dmvp_forw_mex")(*args)[:, 0]) <= 1e-13
+    Ht, idt = SB.htransp(H, idx)
+    assert np.array_equal(idt, -idx)
+    assert _rel(SB.band_mvp(np.conj(Ht), idt, x), M.load_reference("Helm3dmvp_adj_mex")(*args)[:, 0]) <= 1e-13
+
+
+def test_band_oracle_against_compiled_band_gateways():
+    rng, wn, h, npml = _problem(2, n=(8, 7, 9))
+    N = wn.size
+    H, idx = SB.helmholtz_3d_bands(wn, h, npml)
+    X = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    B = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    ref = M.load_reference("Hmvp_MT_mex")(H, idx.astype(float), X, 2.0)
+    assert _rel(SB.band_mvp(H, idx, X), ref) <= 4e-16
+    rn = SB.row_norms_sq(H)
+    swp = M.load_reference("sweep_MT_mex")(H, idx.astype(float), X, B, 1.3, rn)
+    assert np.array_equal(SB.band_sweep(H, idx, X, B, 1.3, rn), swp)
+
+
+def test_band_sweep_equals_matrix_free_sweep():
+    rng, wn, h, npml = _problem(3)
+    n = wn.shape
+    N = wn.size
+    H, idx = SB.helmholtz_3d_bands(wn, h, npml)
+    x = rng.standard_normal((N, 1)) + 1j * rng.standard_normal((N, 1))
+    b = rng.standard_normal((N, 1)) + 1j * rng.standard_normal((N, 1))
+    band = SB.band_sweep(H, idx, x, b, 1.5, SB.row_norms_sq(H))
+    mf = M.load_reference("Helm3d_kacz_sweep_mex")(wn.reshape(-1, order="F"), h, np.array(n, float), npml, 1.5, x, b)
+    assert _rel(band, mf) <= 1e-13
