@@ -32,6 +32,10 @@
  *   h3d_axis_apply     grid transfers of the ML_GMRES multigrid preconditioner
  *                      (construct_multigrid.m:45-51, fine2coarse.m:40-55: Kronecker
  *                       products of 1D interpolation operators, one axis per call)
+ *   h3d_band_coefs     the band-storage (mat_free = false) operator: helmholtz_3d.m:35-190
+ *                      (27 x N bands of H) and conj(Htransp(H)) (opBandStorage.m:127-129)
+ *   h3d_band_mvp       Hmvp_MT_mex (Hmvp_MT_mex.c:53-73, via Hmvp.m / opBandStorage.multiply)
+ *   h3d_band_sweep     sweep_MT_mex (sweep_MT_mex.c:55-97, via opBandStorage.kacz_sweep)
  *
  * Every call is asynchronous on the given CUDA stream (NULL = legacy default
  * stream) unless documented otherwise; all pointers are device pointers unless
@@ -256,6 +260,36 @@ int h3d_rec_spread(const h3d_grid *g, const int32_t *base, const double *w, int 
  * (dtype C128 or C64; the sums are formed in double). */
 int h3d_axis_apply(const int32_t *rowptr, const int32_t *col, const double *val, int n_out, int axis,
                    const int32_t dims_in[3], const void *x, void *y, int nrhs, int dtype, void *stream);
+
+/* ---- band storage (the reference's mat_free = false path) ---------------------------- */
+/* A band matrix holds ndiags couplings per row: coef[k + ndiags*i] = A(i, i + offsets[k])
+ * (the reference's ndiags x N column-major array; complex interleaved, device memory).
+ *
+ * h3d_band_coefs: the 27 x N band matrix of the operator the matrix-free entry points
+ * apply (mode FORWARD: H as helmholtz_3d.m:35-190 builds it, couplings to points outside
+ * the grid zero; mode ADJOINT: the band storage of H^H that opBandStorage.m:127-129 forms
+ * as conj(Htransp(H)), band k holding offset -offsets[k] of the forward bands).  wn as for
+ * h3d_mvp; offsets_out: 27 host int64.  The PML follows the grid's npml (lo/hi per axis,
+ * as the matrix-free kernels); helmholtz_3d.m's create_pml reads its 2x3 npml rows the
+ * other way round, which only matters for unequal widths on the two sides of an axis. */
+int h3d_band_coefs(const h3d_grid *g, const void *wn_re, const void *wn_im, int mode, void *coef,
+                   int64_t offsets_out[27], int dtype, void *stream);
+
+/* y = A x for A in band storage with 1 <= ndiags <= 64 and any offsets (host int64);
+ * couplings with i + offsets[k] outside [0, n) are skipped (Hmvp_MT_mex.c:66-71).
+ * x, y: n x nrhs, must not overlap. */
+int h3d_band_mvp(const void *coef, const int64_t *offsets, int ndiags, int64_t n, const void *x,
+                 void *y, int nrhs, int dtype, void *stream);
+
+/* One forward + backward Kaczmarz sweep on band storage (sweep_MT_mex.c:55-97) with
+ * relaxation w, on x in place, right-hand side b (NULL = 0).  The 27 offsets (host int64)
+ * must be the 27-point neighbourhood of grid g (every axis >= 3 points) in any order, and
+ * couplings across a face of the grid must be zero (as h3d_band_coefs and helmholtz_3d.m
+ * produce them): the rows then run as parallel hyperplanes with the sequential result.
+ * row_norms: squared row norms (double for C128, float for C64), or NULL for the sum of
+ * |A(i,k)|^2 over all 27 bands (opBandStorage.m:139-144). */
+int h3d_band_sweep(const h3d_grid *g, const void *coef, const int64_t *offsets, const void *row_norms,
+                   double w, void *x, const void *b, int nrhs, int dtype, void *stream);
 
 #ifdef __cplusplus
 }

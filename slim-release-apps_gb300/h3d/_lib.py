@@ -99,6 +99,10 @@ _SIGS = {
                                  vp]),
     "h3d_axis_apply": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.POINTER(C.c_int32), vp, vp, C.c_int,
                                  C.c_int, vp]),
+    "h3d_band_coefs": (C.c_int, [C.POINTER(Grid), vp, vp, C.c_int, vp, C.POINTER(C.c_int64), C.c_int, vp]),
+    "h3d_band_mvp": (C.c_int, [vp, C.POINTER(C.c_int64), C.c_int, C.c_int64, vp, vp, C.c_int, C.c_int, vp]),
+    "h3d_band_sweep": (C.c_int, [C.POINTER(Grid), vp, C.POINTER(C.c_int64), vp, C.c_double, vp, vp, C.c_int,
+                                 C.c_int, vp]),
 }
 
 EXPORTED = sorted(_SIGS)

@@ -56,10 +56,10 @@ def _worker(rank, world, port, npairs, shape, out):
 @pytest.mark.parametrize("npairs", [5, 1])
 def test_two_rank_sum_matches_serial(npairs):
     shape = (4, 3, 2)
-    mgr = mp.Manager()
+    ctx = mp.get_context("spawn")      # no fork: earlier tests leave OpenMP threads running
+    mgr = ctx.Manager()
     out = mgr.dict()
     port = _free_port()
-    ctx = mp.get_context("spawn")
     procs = [ctx.Process(target=_worker, args=(r, 2, port, npairs, shape, out)) for r in range(2)]
     for p in procs:
         p.start()
