@@ -36,6 +36,8 @@
  *                      (27 x N bands of H) and conj(Htransp(H)) (opBandStorage.m:127-129)
  *   h3d_band_mvp       Hmvp_MT_mex (Hmvp_MT_mex.c:53-73, via Hmvp.m / opBandStorage.multiply)
  *   h3d_band_sweep     sweep_MT_mex (sweep_MT_mex.c:55-97, via opBandStorage.kacz_sweep)
+ *   h3d_mex_band_mvp,  host entries of the drop-in Hmvp_MT_mex / sweep_MT_mex gateways
+ *   h3d_mex_band_sweep (Hmvp_MT_mex.c:76-141, sweep_MT_mex.c:100-188; ibin/install_MEX:75-86)
  *
  * Every call is asynchronous on the given CUDA stream (NULL = legacy default
  * stream) unless documented otherwise; all pointers are device pointers unless
@@ -290,6 +292,20 @@ int h3d_band_mvp(const void *coef, const int64_t *offsets, int ndiags, int64_t n
  * |A(i,k)|^2 over all 27 bands (opBandStorage.m:139-144). */
 int h3d_band_sweep(const h3d_grid *g, const void *coef, const int64_t *offsets, const void *row_norms,
                    double w, void *x, const void *b, int nrhs, int dtype, void *stream);
+
+/* Host entries of the band gateways: MATLAB's split-complex host arrays (coef ndiags x n
+ * column-major, offsets as doubles, x / b / y n x nrhs), synchronous.  Checks as the
+ * reference: x_rows != n and rn_rows != n give H3D_ERR_XSIZE (reported with the reference's
+ * HMvp_MT_mex:NumElements identifier by the gateway).  The sweep takes the 27 bands of a
+ * grid stencil (the grid is read off the offsets) with the row norms given, and returns the
+ * swept copy of x in y. */
+int h3d_mex_band_mvp(const double *coef_re, const double *coef_im, size_t ndiags, size_t n,
+                     const double *offsets, const double *x_re, const double *x_im, size_t x_rows,
+                     size_t nrhs, double *y_re, double *y_im);
+int h3d_mex_band_sweep(const double *coef_re, const double *coef_im, size_t ndiags, size_t n,
+                       const double *offsets, const double *x_re, const double *x_im, size_t x_rows,
+                       size_t nrhs, const double *b_re, const double *b_im, size_t b_rows, double w,
+                       const double *row_norms, size_t rn_rows, double *y_re, double *y_im);
 
 #ifdef __cplusplus
 }

@@ -20,10 +20,13 @@
 //    the grid.  The reference instead adds those zero couplings through its linear bounds
 //    test (a face row's +1 reaches the next line's first point): the values are the same,
 //    and skipping them keeps two rows of one hyperplane from writing the same point.
+#include <algorithm>
 #include <cmath>
+#include <cstring>
 
 #include "h3d_internal.cuh"
 #include "h3d_kernels.cuh"
+#include "h3d_vec.cuh"
 
 namespace h3d {
 
@@ -271,5 +274,164 @@ extern "C" int h3d_band_sweep(const h3d_grid *g, const void *coef, const int64_t
         }
     }
     H3D_CUDA_TRY(cudaGetLastError());
+    return H3D_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// Host entries of the drop-in band gateways (Hmvp_MT_mex.c:76-141, sweep_MT_mex.c:100-188):
+// MATLAB's split-complex column-major arrays in host memory, copied to the device,
+// interleaved, processed, copied back.
+
+namespace h3d {
+
+static int offsets_from_mex(const double *offsets, size_t ndiags, int64_t *off)
+{
+    for (size_t k = 0; k < ndiags; ++k) {
+        const double v = offsets[k];
+        if (!std::isfinite(v) || v != std::floor(v) || std::fabs(v) > 9.0e15) {
+            set_error("offset %zu is not an integer", k);
+            return H3D_ERR_BAD_ARG;
+        }
+        off[k] = (int64_t)v;
+    }
+    return H3D_OK;
+}
+
+// Split (re, im) host planes of n values -> interleaved device buffer (im may be NULL).
+static int upload_split(const double *re, const double *im, long long n, DevBuf &stage, DevBuf &out, cudaStream_t st)
+{
+    int rc;
+    const size_t pb = (size_t)n * sizeof(double);
+    if ((rc = stage.alloc(2 * pb, st)) || (rc = out.alloc(2 * pb, st))) return rc;
+    double *pre = stage.as<double>(), *pim = pre + n;
+    H3D_CUDA_TRY(cudaMemcpyAsync(pre, re, pb, cudaMemcpyHostToDevice, st));
+    if (im) H3D_CUDA_TRY(cudaMemcpyAsync(pim, im, pb, cudaMemcpyHostToDevice, st));
+    return interleave<double>(pre, im ? pim : nullptr, out.as<cplx<double>>(), n, st);
+}
+
+static int download_split(const DevBuf &in, long long n, DevBuf &stage, double *re, double *im, cudaStream_t st)
+{
+    int rc;
+    const size_t pb = (size_t)n * sizeof(double);
+    if ((rc = stage.alloc(2 * pb, st))) return rc;
+    double *pre = stage.as<double>(), *pim = pre + n;
+    if ((rc = deinterleave<double>(in.as<cplx<double>>(), pre, pim, n, st))) return rc;
+    H3D_CUDA_TRY(cudaMemcpyAsync(re, pre, pb, cudaMemcpyDeviceToHost, st));
+    H3D_CUDA_TRY(cudaMemcpyAsync(im, pim, pb, cudaMemcpyDeviceToHost, st));
+    return H3D_OK;
+}
+
+// The grid of a 27-point band matrix from its offsets: the positive offsets in ascending
+// order are 1, nx-1, nx, nx+1, nxy-nx-1, ..., nxy, ... (every axis >= 3 points), so nx is the
+// third and nx*ny the ninth.
+static int grid_from_offsets(const int64_t *off, long long n, h3d_grid *g)
+{
+    long long pos[27];
+    int np = 0;
+    for (int k = 0; k < 27; ++k)
+        if (off[k] > 0) pos[np++] = off[k];
+    if (np != 13) {
+        set_error("the 27 offsets are not a 27-point grid neighbourhood");
+        return H3D_ERR_BAD_ARG;
+    }
+    std::sort(pos, pos + np);
+    const long long nx = pos[2], nxy = pos[8];
+    if (nx < 3 || nxy % nx != 0 || nxy / nx < 3 || n % nxy != 0 || n / nxy < 3 || n / nxy > 0x7fffffffLL ||
+        nxy / nx > 0x7fffffffLL || nx > 0x7fffffffLL) {
+        set_error("the 27 offsets are not the neighbourhood of a grid of n = %lld points", n);
+        return H3D_ERR_BAD_ARG;
+    }
+    std::memset(g, 0, sizeof *g);
+    g->n[0] = (int32_t)nx;
+    g->n[1] = (int32_t)(nxy / nx);
+    g->n[2] = (int32_t)(n / nxy);
+    g->h[0] = g->h[1] = g->h[2] = 1.0;  // the band sweep reads only the sizes
+    return H3D_OK;
+}
+
+}  // namespace h3d
+
+extern "C" int h3d_mex_band_mvp(const double *coef_re, const double *coef_im, size_t ndiags, size_t n,
+                                const double *offsets, const double *x_re, const double *x_im, size_t x_rows,
+                                size_t nrhs, double *y_re, double *y_im)
+{
+    if (x_rows != n) {
+        set_error("The row size of the vector x and the column size of the matrix A must match");
+        return H3D_ERR_XSIZE;
+    }
+    if (!coef_re || !offsets || !x_re || !y_re || !y_im || ndiags < 1 || ndiags > (size_t)kMaxBands || n < 1 ||
+        nrhs < 1 || nrhs > 65535) {
+        set_error("h3d_mex_band_mvp: bad argument");
+        return H3D_ERR_BAD_ARG;
+    }
+    int64_t off[kMaxBands];
+    int rc = offsets_from_mex(offsets, ndiags, off);
+    if (rc) return rc;
+    cudaStream_t st = nullptr;
+    H3D_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    rc = [&]() -> int {
+        DevBuf sc, dc, sx, dx, dy, sy;
+        const long long nc = (long long)ndiags * (long long)n, nv = (long long)n * (long long)nrhs;
+        int r;
+        if ((r = upload_split(coef_re, coef_im, nc, sc, dc, st))) return r;
+        sc.release();
+        if ((r = upload_split(x_re, x_im, nv, sx, dx, st))) return r;
+        if ((r = dy.alloc((size_t)nv * sizeof(cplx<double>), st))) return r;
+        if ((r = h3d_band_mvp(dc.p, off, (int)ndiags, (int64_t)n, dx.p, dy.p, (int)nrhs, H3D_C128, st))) return r;
+        return download_split(dy, nv, sy, y_re, y_im, st);
+    }();
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "h3d_mex_band_mvp");
+    return H3D_OK;
+}
+
+extern "C" int h3d_mex_band_sweep(const double *coef_re, const double *coef_im, size_t ndiags, size_t n,
+                                  const double *offsets, const double *x_re, const double *x_im, size_t x_rows,
+                                  size_t nrhs, const double *b_re, const double *b_im, size_t b_rows, double w,
+                                  const double *row_norms, size_t rn_rows, double *y_re, double *y_im)
+{
+    if (x_rows != n) {
+        set_error("The row size of the vector x and the column size of the matrix A must match");
+        return H3D_ERR_XSIZE;
+    }
+    if (b_rows != n) {
+        set_error("b must have N rows");
+        return H3D_ERR_BSIZE;
+    }
+    if (rn_rows != n) {
+        set_error("The size of the row norms vector and the rows size of the matrix A must match");
+        return H3D_ERR_XSIZE;
+    }
+    if (!coef_re || !offsets || !x_re || !b_re || !row_norms || !y_re || !y_im || ndiags != 27 || n < 27 ||
+        nrhs < 1 || !std::isfinite(w)) {
+        set_error("h3d_mex_band_sweep: bad argument (the GPU band sweep takes the 27 bands of a grid stencil)");
+        return H3D_ERR_BAD_ARG;
+    }
+    int64_t off[27];
+    int rc = offsets_from_mex(offsets, 27, off);
+    if (rc) return rc;
+    h3d_grid g;
+    if ((rc = grid_from_offsets(off, (long long)n, &g))) return rc;
+    cudaStream_t st = nullptr;
+    H3D_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    rc = [&]() -> int {
+        DevBuf sc, dc, sx, dx, sb, db, rn, sy;
+        const long long nc = 27LL * (long long)n, nv = (long long)n * (long long)nrhs;
+        int r;
+        if ((r = upload_split(coef_re, coef_im, nc, sc, dc, st))) return r;
+        sc.release();
+        if ((r = upload_split(x_re, x_im, nv, sx, dx, st))) return r;
+        if ((r = upload_split(b_re, b_im, nv, sb, db, st))) return r;
+        if ((r = rn.alloc((size_t)n * sizeof(double), st))) return r;
+        H3D_CUDA_TRY(cudaMemcpyAsync(rn.p, row_norms, (size_t)n * sizeof(double), cudaMemcpyHostToDevice, st));
+        if ((r = h3d_band_sweep(&g, dc.p, off, rn.p, w, dx.p, db.p, (int)nrhs, H3D_C128, st))) return r;
+        return download_split(dx, nv, sy, y_re, y_im, st);
+    }();
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "h3d_mex_band_sweep");
     return H3D_OK;
 }

@@ -103,6 +103,10 @@ _SIGS = {
     "h3d_band_mvp": (C.c_int, [vp, C.POINTER(C.c_int64), C.c_int, C.c_int64, vp, vp, C.c_int, C.c_int, vp]),
     "h3d_band_sweep": (C.c_int, [C.POINTER(Grid), vp, C.POINTER(C.c_int64), vp, C.c_double, vp, vp, C.c_int,
                                  C.c_int, vp]),
+    "h3d_mex_band_mvp": (C.c_int, [dp, dp, C.c_size_t, C.c_size_t, dp, dp, dp, C.c_size_t, C.c_size_t, dp,
+                                   dp]),
+    "h3d_mex_band_sweep": (C.c_int, [dp, dp, C.c_size_t, C.c_size_t, dp, dp, dp, C.c_size_t, C.c_size_t, dp,
+                                     dp, C.c_size_t, C.c_double, dp, C.c_size_t, dp, dp]),
 }
 
 EXPORTED = sorted(_SIGS)

@@ -44,6 +44,9 @@ MEX_VARIANTS = {
     "Helm3d_kacz_sweep_mex": ("swp", []),
     "Helm3d_kacz_sweep_wnc_mex": ("swp", ["-DWNCMPLX"]),
     "Helm3d_kacz_sweep_adj_mex": ("swp", ["-DADJ"]),
+    # the band-storage gateways, install_MEX:75-86
+    "Hmvp_MT_mex": ("bmvp", []),
+    "sweep_MT_mex": ("bswp", []),
 }
 
 
@@ -106,7 +109,8 @@ def build_mex(verbose: bool = False, force: bool = False) -> dict:
         out[name] = so
         if not force and _newer(so, [gw, stub_c, LIB, os.path.join(INCLUDE, "h3d.h")]):
             continue
-        kflag = "-DH3D_GATEWAY_MVP" if kind == "mvp" else "-DH3D_GATEWAY_SWEEP"
+        kflag = {"mvp": "-DH3D_GATEWAY_MVP", "swp": "-DH3D_GATEWAY_SWEEP", "bmvp": "-DH3D_GATEWAY_BAND_MVP",
+                 "bswp": "-DH3D_GATEWAY_BAND_SWEEP"}[kind]
         _run([cc, "-O2", "-std=c11", "-fPIC", "-shared", kflag, *flags, "-I", INCLUDE, "-I",
               stub_dir, gw, stub_c, "-o", so, "-L", LIBDIR, "-lh3d",
               "-Wl,-rpath,$ORIGIN/.."], verbose)

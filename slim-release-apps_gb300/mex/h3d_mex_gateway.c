@@ -8,6 +8,10 @@
  *       y = Helm3dmvp_xxx_mex(wn, h, n, npml, x, nthreads)       (Helm3dmvp_mex.c:17-48)
  *   -DH3D_GATEWAY_SWEEP [-DADJ] [-DWNCMPLX]            -> Helm3d_kacz_sweep_*_mex
  *       y = Helm3d_kacz_sweep_xxx_mex(wn, h, n, npml, w, x, b)   (Helm3dkaczswp_mex.c:21-50)
+ *   -DH3D_GATEWAY_BAND_MVP                             -> Hmvp_MT_mex (install_MEX:75-76)
+ *       y = Hmvp_MT_mex(coef, offset, x, nthreads)               (Hmvp_MT_mex.c:12-45)
+ *   -DH3D_GATEWAY_BAND_SWEEP                           -> sweep_MT_mex (install_MEX:78-86)
+ *       y = sweep_MT_mex(coef, offset, x, b, w, row_norms_sq)    (sweep_MT_mex.c:12-47)
  *
  * Same argument order, same checks and error identifiers as the reference
  * gateways, same output (a new N x 1 or N x P complex double matrix).  The
@@ -19,7 +23,10 @@
  *   - Helm3d_kacz_sweep_wnc_mex uses the imaginary part of wn (the reference's
  *     install line spells the flag -DWNCMPLEX, so its build silently drops it);
  *   - a b with fewer columns than x is rejected with the Bsize identifier instead
- *     of being read out of bounds.
+ *     of being read out of bounds;
+ *   - sweep_MT_mex takes the 27 bands of a grid stencil (as helmholtz_3d.m builds them;
+ *     the grid is read off the offsets), which the GPU sweeps as parallel hyperplanes;
+ *     other band matrices are rejected.
  */
 #include <stddef.h>
 #include <stdio.h>
@@ -136,6 +143,69 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
     if (rc != H3D_OK) fail(rc, "Helm3dkaczswp_mex");
 }
 
+#elif defined(H3D_GATEWAY_BAND_MVP) || defined(H3D_GATEWAY_BAND_SWEEP)
+
+#define BAND_ID ID_PREFIX "HMvp_MT_mex:NumElements"
+
+static void band_fail(int status)
+{
+    if (status == H3D_ERR_XSIZE || status == H3D_ERR_BSIZE)
+        mexErrMsgIdAndTxt(BAND_ID, "%s", h3d_last_error());
+    else
+        mexErrMsgIdAndTxt(h3d_status_id(status), "%s", h3d_last_error());
+}
+
+#if defined(H3D_GATEWAY_BAND_MVP)
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
+{
+    (void)nlhs;
+    if (nrhs < 3) mexErrMsgIdAndTxt("h3d:badArgument", "expected (coef,offset,x[,nthreads])");
+    const mxArray *COEF = prhs[0], *OFF = prhs[1], *X = prhs[2];
+    const size_t n = mxGetN(COEF), nd = mxGetM(COEF);
+    if (mxGetM(X) != n) {
+        mexErrMsgIdAndTxt(BAND_ID, "The row size of the vector x and the column size of the matrix A must match");
+        return;
+    }
+    const size_t P = mxGetN(X);
+    plhs[0] = mxCreateDoubleMatrix(n, P, mxCOMPLEX);
+    int rc = h3d_mex_band_mvp(mxGetPr(COEF), mxIsComplex(COEF) ? mxGetPi(COEF) : NULL, nd, n, mxGetPr(OFF),
+                              mxGetPr(X), mxIsComplex(X) ? mxGetPi(X) : NULL, mxGetM(X), P, mxGetPr(plhs[0]),
+                              mxGetPi(plhs[0]));
+    if (rc != H3D_OK) band_fail(rc);
+}
+
 #else
-#error "define H3D_GATEWAY_MVP or H3D_GATEWAY_SWEEP"
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
+{
+    (void)nlhs;
+    if (nrhs < 6) mexErrMsgIdAndTxt("h3d:badArgument", "expected (coef,offset,x,b,w,row_norms_sq)");
+    const mxArray *COEF = prhs[0], *OFF = prhs[1], *X = prhs[2], *B = prhs[3], *OMEGA = prhs[4], *RN = prhs[5];
+    const size_t n = mxGetN(COEF), nd = mxGetM(COEF);
+    if (mxGetM(X) != n) {
+        mexErrMsgIdAndTxt(BAND_ID, "The row size of the vector x and the column size of the matrix A must match");
+        return;
+    }
+    if (mxGetM(RN) != n) {
+        mexErrMsgIdAndTxt(BAND_ID, "The size of the row norms vector and the rows size of the matrix A must match");
+        return;
+    }
+    const size_t P = mxGetN(X);
+    if (mxGetM(B) != n || mxGetN(B) < P) {
+        mexErrMsgIdAndTxt(BAND_ID, "b must have as many rows as x and at least as many columns");
+        return;
+    }
+    plhs[0] = mxCreateDoubleMatrix(n, P, mxCOMPLEX);
+    int rc = h3d_mex_band_sweep(mxGetPr(COEF), mxIsComplex(COEF) ? mxGetPi(COEF) : NULL, nd, n, mxGetPr(OFF),
+                                mxGetPr(X), mxIsComplex(X) ? mxGetPi(X) : NULL, mxGetM(X), P, mxGetPr(B),
+                                mxIsComplex(B) ? mxGetPi(B) : NULL, mxGetM(B), mxGetScalar(OMEGA), mxGetPr(RN),
+                                mxGetM(RN), mxGetPr(plhs[0]), mxGetPi(plhs[0]));
+    if (rc != H3D_OK) band_fail(rc);
+}
+
+#endif
+
+#else
+#error "define H3D_GATEWAY_MVP, H3D_GATEWAY_SWEEP, H3D_GATEWAY_BAND_MVP or H3D_GATEWAY_BAND_SWEEP"
 #endif

@@ -71,3 +71,29 @@ def test_band_sweep_equals_matrix_free_sweep():
     band = SB.band_sweep(H, idx, x, b, 1.5, SB.row_norms_sq(H))
     mf = M.load_reference("Helm3d_kacz_sweep_mex")(wn.reshape(-1, order="F"), h, np.array(n, float), npml, 1.5, x, b)
     assert _rel(band, mf) <= 1e-13
+
+
+def test_band_gateways_check_sizes_like_the_reference():
+    """The drop-in Hmvp_MT_mex / sweep_MT_mex refuse mismatched sizes with the reference's
+    identifier before any device work (Hmvp_MT_mex.c:105-109, sweep_MT_mex.c:134-160)."""
+    from h3d import build
+
+    gws = build.build_mex()
+    rng, wn, h, npml = _problem(4)
+    N = wn.size
+    H, idx = SB.helmholtz_3d_bands(wn, h, npml)
+    x = rng.standard_normal((N, 1)) + 0j
+    ident = "SLIM_release_apps:tools:algorithms:ThreeDFreqModeling:HMvp_MT_mex:NumElements"
+    for lib in (gws["Hmvp_MT_mex"], os.path.join(M.REF_DIR, "Hmvp_MT_mex.so")):
+        with pytest.raises(M.MexError) as e:
+            M.MexFunction(lib)(H, idx.astype(float), x[:-1], 1.0)
+        assert e.value.ident == ident
+    rn = SB.row_norms_sq(H)
+    for lib in (gws["sweep_MT_mex"], os.path.join(M.REF_DIR, "sweep_MT_mex.so")):
+        f = M.MexFunction(lib)
+        with pytest.raises(M.MexError) as e:
+            f(H, idx.astype(float), x[:-1], x, 1.5, rn)
+        assert e.value.ident == ident
+        with pytest.raises(M.MexError) as e:
+            f(H, idx.astype(float), x, x, 1.5, rn[:-1])
+        assert e.value.ident == ident

@@ -150,3 +150,22 @@ def test_band_sweep_refuses_foreign_offsets(cuda):
                                  C.c_void_p(torch.cuda.current_stream().cuda_stream))
     assert rc == L.ERR_BAD_ARG
     assert b"neighbourhood" in L.load().h3d_last_error()
+
+
+def test_band_gateways_drop_in(cuda):
+    """Hmvp_MT_mex / sweep_MT_mex gateways (same names and arguments as the reference
+    binaries) against the band oracle, itself pinned to the compiled reference gateways."""
+    from h3d import build
+    from oracle import mexharness as M
+
+    gws = build.build_mex()
+    rng, grid, wn, wn3, h, npml23 = _problem(cuda, n=(9, 8, 10), seed=11)
+    H, idx = SB.helmholtz_3d_bands(wn3, h, npml23)
+    N = H.shape[1]
+    X = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    B = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    y = M.MexFunction(gws["Hmvp_MT_mex"])(H, idx.astype(float), X, 2.0)
+    assert _rel(y, SB.band_mvp(H, idx, X)) <= 1e-14
+    rn = SB.row_norms_sq(H)
+    ys = M.MexFunction(gws["sweep_MT_mex"])(H, idx.astype(float), X, B, 1.4, rn)
+    assert _rel(ys, SB.band_sweep(H, idx, X, B, 1.4, rn)) <= 1e-12
