@@ -346,6 +346,17 @@ static int grid_from_offsets(const int64_t *off, long long n, h3d_grid *g)
     g->n[1] = (int32_t)(nxy / nx);
     g->n[2] = (int32_t)(n / nxy);
     g->h[0] = g->h[1] = g->h[2] = 1.0;  // the band sweep reads only the sizes
+    // all 27 offsets must be that grid's (checked here, before any device work)
+    long long want[27], have[27];
+    grid_offsets(g, want);
+    for (int k = 0; k < 27; ++k) have[k] = off[k];
+    std::sort(want, want + 27);
+    std::sort(have, have + 27);
+    for (int k = 0; k < 27; ++k)
+        if (want[k] != have[k]) {
+            set_error("the 27 offsets are not the neighbourhood of a grid of n = %lld points", n);
+            return H3D_ERR_BAD_ARG;
+        }
     return H3D_OK;
 }
 

@@ -97,3 +97,40 @@ def test_band_gateways_check_sizes_like_the_reference():
         with pytest.raises(M.MexError) as e:
             f(H, idx.astype(float), x, x, 1.5, rn[:-1])
         assert e.value.ident == ident
+
+
+def test_band_sweep_gateway_reads_the_grid_off_the_offsets():
+    """h3d_mex_band_sweep refuses, before any device work, bands that are not the 27-point
+    stencil of a grid of at least 3 points per axis (host arrays only)."""
+    import ctypes as C
+
+    from h3d import _lib as L
+
+    lib = L.load()
+    rng, wn, h, npml = _problem(5)
+    N = wn.size
+    H, idx = SB.helmholtz_3d_bands(wn, h, npml)
+    x = np.zeros(N)
+    rn = SB.row_norms_sq(H)
+    yr, yi = np.zeros(N), np.zeros(N)
+    p = lambda a: np.ascontiguousarray(a, dtype=np.float64).ctypes.data_as(C.POINTER(C.c_double))
+    Hr, Hi = np.asfortranarray(H.real), np.asfortranarray(H.imag)
+
+    def call(off, nd=27):
+        return lib.h3d_mex_band_sweep(p(Hr), p(Hi), nd, N, p(off), p(x), None, N, 1, p(x), None, N, 1.5, p(rn), N,
+                                      p(yr), p(yi))
+
+    bad = idx.astype(float)
+    bad[3] += 0.5                                  # not an integer
+    assert call(bad) == L.ERR_BAD_ARG
+    bad = idx.astype(float)
+    bad[20] = 7.0                                  # not a grid neighbourhood
+    assert call(bad) == L.ERR_BAD_ARG and b"neighbourhood" in lib.h3d_last_error()
+    assert call(idx.astype(float), nd=26) == L.ERR_BAD_ARG
+    # a 2-point axis: its offsets collide with another axis' (refused)
+    H2, idx2 = SB.helmholtz_3d_bands(np.ones((5, 2, 6)), h, np.zeros((2, 3)))
+    N2 = H2.shape[1]
+    x2, rn2 = np.zeros(N2), SB.row_norms_sq(H2)
+    rc = lib.h3d_mex_band_sweep(p(H2.real), p(H2.imag), 27, N2, p(idx2.astype(float)), p(x2), None, N2, 1, p(x2),
+                                None, N2, 1.5, p(rn2), N2, p(x2), p(x2))
+    assert rc == L.ERR_BAD_ARG
