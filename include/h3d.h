@@ -271,9 +271,10 @@ int h3d_axis_apply(const int32_t *rowptr, const int32_t *col, const double *val,
  * apply (mode FORWARD: H as helmholtz_3d.m:35-190 builds it, couplings to points outside
  * the grid zero; mode ADJOINT: the band storage of H^H that opBandStorage.m:127-129 forms
  * as conj(Htransp(H)), band k holding offset -offsets[k] of the forward bands).  wn as for
- * h3d_mvp; offsets_out: 27 host int64.  The PML follows the grid's npml (lo/hi per axis,
- * as the matrix-free kernels); helmholtz_3d.m's create_pml reads its 2x3 npml rows the
- * other way round, which only matters for unequal widths on the two sides of an axis. */
+ * h3d_mvp; offsets_out: 27 host int64.  The bands are those of the matrix-free operator;
+ * helmholtz_3d.m builds the same matrix for equal PML widths on the two sides of each axis,
+ * and a different one for unequal widths (create_pml.m reads the 2x3 npml rows the other way
+ * round and its profile differs from the matrix-free PML functions there). */
 int h3d_band_coefs(const h3d_grid *g, const void *wn_re, const void *wn_im, int mode, void *coef,
                    int64_t offsets_out[27], int dtype, void *stream);
 

@@ -134,3 +134,26 @@ def test_band_sweep_gateway_reads_the_grid_off_the_offsets():
     rc = lib.h3d_mex_band_sweep(p(H2.real), p(H2.imag), 27, N2, p(idx2.astype(float)), p(x2), None, N2, 1, p(x2),
                                 None, N2, 1.5, p(rn2), N2, p(x2), p(x2))
     assert rc == L.ERR_BAD_ARG
+
+
+def test_band_and_matrix_free_paths_differ_for_unequal_pml_widths():
+    """The two reference paths build the same operator only for equal PML widths on the two
+    sides of an axis (every workload here).  For unequal widths they differ whichever way
+    the 2 x 3 npml rows are read: create_pml.m:47-52 takes np(2,a) as the lower width and
+    np(1,a) as the upper one, while the matrix-free PML functions (Helm3d_27pt.h:326-390)
+    test the interior against the lower width on both sides.  The library's band
+    coefficients follow the matrix-free operator."""
+    rng, wn, h, _ = _problem(6, n=(10, 9, 8))
+    n = wn.shape
+    N = wn.size
+    npml = np.array([[3.0, 1.0, 2.0], [1.0, 3.0, 4.0]])
+    H, idx = SB.helmholtz_3d_bands(wn, h, npml)
+    x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    y = SB.band_mvp(H, idx, x)
+    mv = M.load_reference("Helm3dmvp_forw_mex")
+    args = lambda p: (wn.reshape(-1, order="F"), h, np.array(n, float), p, x, 1.0)
+    assert _rel(y, mv(*args(npml))[:, 0]) > 1e-3
+    assert _rel(y, mv(*args(npml[::-1].copy()))[:, 0]) > 1e-3
+    sym = np.array([[2.0, 3.0, 1.0], [2.0, 3.0, 1.0]])
+    Hs, idxs = SB.helmholtz_3d_bands(wn, h, sym)
+    assert _rel(SB.band_mvp(Hs, idxs, x), mv(*args(sym))[:, 0]) <= 1e-13
