@@ -12,7 +12,8 @@
 //
 // Against the COLOUR27 order (27 grid-wide launches per pass, each re-reading its footprint
 // boxes), x and the wavenumber cross HBM/L2 about once per pass (plus the one-point halo),
-// and a pass is 8 launches.  With block sides divisible by 3 every colour has the same
+// and a pass is 8 parity phases (a double sweep 15 launches: the forward pass's last parity
+// runs its colours up and back down in one launch).  With block sides divisible by 3 every colour has the same
 // (BX/3)(BY/3)(BZ/3) rows in a block (fewer at the grid's far faces), so thread t owns one
 // fixed (row, right-hand side) slot for all colours: no index division in the colour loop.
 //
