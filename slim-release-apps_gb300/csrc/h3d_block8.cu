@@ -12,10 +12,11 @@
 //
 // Against the COLOUR27 order (27 grid-wide launches per pass, each re-reading its footprint
 // boxes), x and the wavenumber cross HBM/L2 about once per pass (plus the one-point halo),
-// and a pass is 8 parity phases (a double sweep 15 launches: the forward pass's last parity
-// runs its colours up and back down in one launch).  With block sides divisible by 3 every colour has the same
-// (BX/3)(BY/3)(BZ/3) rows in a block (fewer at the grid's far faces), so thread t owns one
-// fixed (row, right-hand side) slot for all colours: no index division in the colour loop.
+// and a pass is 8 parity phases (a double sweep 15 launches: the forward pass's last
+// parity runs its colours up and back down in one launch).  With block sides divisible by 3
+// every colour has the same (BX/3)(BY/3)(BZ/3) rows in a block (fewer at the grid's far
+// faces), so thread t owns one fixed (row, right-hand side) slot for all colours: no index
+// division in the colour loop.
 //
 // Stored coefficients (12x12x12 blocks): the 27 coefficients of every row are formed once
 // per operator (coef8_store_kernel) and kept block- and colour-major, so the coefficients of
