@@ -38,3 +38,11 @@ def golden_small():
     import numpy as np
 
     return dict(np.load(os.path.join(GOLDEN, "stencil_small.npz")))
+
+
+@pytest.fixture(scope="session")
+def golden_band():
+    """Band-storage goldens from the compiled Hmvp_MT_mex / sweep_MT_mex (make_golden.py)."""
+    import numpy as np
+
+    return dict(np.load(os.path.join(GOLDEN, "band_small.npz")))

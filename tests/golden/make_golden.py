@@ -18,6 +18,13 @@ What is produced (all from seeded inputs, stored with the inputs):
   regenerated from the seed, so the file stores a checksum of the input, the
   output at 4096 seeded sample indices, its 2-norm and its inner product with a
   seeded probe vector.
+* ``band_small.npz`` -- the band-storage path on a 7x6x8 grid (PML 2): the 27 x N
+  band matrix of helmholtz_3d.m (from oracle/slim_band.py, which MATLAB would be
+  needed to run directly; pinned to the compiled matrix-free gateways), its adjoint
+  bands, and the outputs of the compiled ``Hmvp_MT_mex`` and ``sweep_MT_mex``
+  (forward and adjoint bands, 2 right-hand sides).
+
+``python tests/golden/make_golden.py band`` writes only ``band_small.npz``.
 """
 from __future__ import annotations
 
@@ -102,9 +109,40 @@ def config0_case(out):
         out[f"{tag}/probe_dot"] = np.array(np.vdot(probe, val))
 
 
+def band_case(out):
+    from oracle import slim_band as SB
+
+    rng = np.random.default_rng(31)
+    n, h = (7, 6, 8), (20.0, 25.0, 15.0)
+    npml = np.full((2, 3), 2.0)
+    wn3 = (2 * np.pi * 4.0) ** 2 / (1500.0 + 2000.0 * rng.random(n)) ** 2
+    H, idx = SB.helmholtz_3d_bands(wn3, h, npml)
+    Ha, idxa = SB.htransp(H, idx)
+    Ha = np.conj(Ha)
+    N = H.shape[1]
+    X = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    B = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    mv, sw = M.load_reference("Hmvp_MT_mex"), M.load_reference("sweep_MT_mex")
+    out["n"], out["h"], out["npml"] = np.array(n, float), np.array(h, float), npml
+    out["wn"] = wn3.reshape(-1, order="F")
+    out["H"], out["idx"], out["Hadj"], out["idxadj"] = H, idx, Ha, idxa
+    out["X"], out["B"] = X, B
+    for tag, (A, o) in (("forw", (H, idx)), ("adj", (Ha, idxa))):
+        rn = SB.row_norms_sq(A)
+        out[f"{tag}/rn"] = rn
+        out[f"{tag}/mvp"] = mv(A, o.astype(float), X, 2.0)
+        out[f"{tag}/swp"] = sw(A, o.astype(float), X, B, 1.3, rn)
+
+
 def main():
     if not M.reference_available():
         raise SystemExit("reference gateways missing: run `make -C oracle ref` first")
+    band: dict = {}
+    band_case(band)
+    np.savez_compressed(os.path.join(HERE, "band_small.npz"), **band)
+    if sys.argv[1:] == ["band"]:
+        print("wrote band_small.npz")
+        return
     small: dict = {}
     small_case("g7", (7, 6, 5), (25.0, 25.0, 25.0), [[2, 2, 2], [2, 2, 2]], 11, small)
     small_case("g12", (12, 11, 10), (25.0, 20.0, 15.0), [[3, 2, 3], [2, 3, 1]], 12, small)

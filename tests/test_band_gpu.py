@@ -169,3 +169,27 @@ def test_band_gateways_drop_in(cuda):
     rn = SB.row_norms_sq(H)
     ys = M.MexFunction(gws["sweep_MT_mex"])(H, idx.astype(float), X, B, 1.4, rn)
     assert _rel(ys, SB.band_sweep(H, idx, X, B, 1.4, rn)) <= 1e-12
+
+
+def test_band_path_against_reference_golden(cuda, golden_band):
+    """GPU band coefficients, gateways and BandOp against the committed outputs of the
+    compiled Hmvp_MT_mex / sweep_MT_mex (tests/golden/band_small.npz)."""
+    import torch
+    from h3d import _lib as L
+    from h3d import build
+    from h3d.band import BandOp
+    from oracle import mexharness as M
+
+    g = golden_band
+    n = tuple(int(v) for v in g["n"])
+    grid = L.make_grid(n, tuple(g["h"]), int(g["npml"][0, 0]))
+    wn = torch.as_tensor(g["wn"], device=cuda)
+    for mode, key in ((1, "H"), (2, "Hadj")):
+        A = BandOp.helmholtz(grid, wn, mode=mode)
+        assert _rel(A.coef.cpu().numpy(), g[key].T) <= 1e-13
+    gws = build.build_mex()
+    for tag, A, o in (("forw", g["H"], g["idx"]), ("adj", g["Hadj"], g["idxadj"])):
+        y = M.MexFunction(gws["Hmvp_MT_mex"])(A, o.astype(float), g["X"], 2.0)
+        assert _rel(y, g[f"{tag}/mvp"]) <= 1e-14
+        ys = M.MexFunction(gws["sweep_MT_mex"])(A, o.astype(float), g["X"], g["B"], 1.3, g[f"{tag}/rn"])
+        assert _rel(ys, g[f"{tag}/swp"]) <= 1e-12

@@ -129,3 +129,17 @@ def test_config0_golden_input_checksums():
     m = models.config0()
     wn = m.wavenumber()
     np.testing.assert_allclose([wn.sum(), np.linalg.norm(wn), wn.min(), wn.max()], c0["wn_checksum"], rtol=1e-12)
+
+
+def test_band_oracle_matches_reference_golden(golden_band):
+    """oracle/slim_band.py against the committed outputs of the compiled band gateways."""
+    from oracle import slim_band as SB
+
+    g = golden_band
+    n = tuple(int(v) for v in g["n"])
+    H, idx = SB.helmholtz_3d_bands(g["wn"].reshape(n, order="F"), g["h"], g["npml"])
+    assert np.array_equal(H, g["H"]) and np.array_equal(idx, g["idx"])
+    for tag, A, o in (("forw", g["H"], g["idx"]), ("adj", g["Hadj"], g["idxadj"])):
+        y = SB.band_mvp(A, o, g["X"])
+        assert np.abs(y - g[f"{tag}/mvp"]).max() <= 4e-16 * np.abs(g[f"{tag}/mvp"]).max()
+        assert np.array_equal(SB.band_sweep(A, o, g["X"], g["B"], 1.3, g[f"{tag}/rn"]), g[f"{tag}/swp"])
