@@ -26,3 +26,23 @@ def test_cgmn_and_crmn_solve_hpd_systems():
     assert np.array_equal(x_cr, x_cr0)      # A 0 = 0 exactly: both starts give the same iterates
     # conjugate residual minimises ||r|| over the Krylov space: its history never increases
     assert np.all(np.diff(h_cr) <= 1e-12)
+
+
+def test_cgmn_and_crmn_restatements_match_scipy_cg_and_minres():
+    """On a Hermitian positive definite system (what I - Q is), CGMN.m's iterates are CG's and
+    CRMN.m's are the minimal-residual iterates MINRES also produces: the oracle's
+    restatements equal scipy's independent CG / MINRES after the same iteration count."""
+    from scipy.sparse.linalg import cg, minres
+
+    rng = np.random.default_rng(0)
+    n = 30
+    B = rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))
+    A = B.conj().T @ B / n + 0.5 * np.eye(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    for k in (3, 7, 12):
+        ref, _ = cg(A, b, rtol=1e-30, atol=0.0, maxiter=k)
+        x, _ = slim_ref.cgmn(lambda y: A @ y, b, np.zeros(n, complex), tol=1e-30, maxit=k)
+        assert np.linalg.norm(x - ref) <= 1e-13 * np.linalg.norm(ref)
+        ref, _ = minres(A, b, rtol=1e-30, maxiter=k)
+        x, _ = slim_ref.crmn(lambda y: A @ y, b, np.zeros(n, complex), tol=1e-30, maxit=k)
+        assert np.linalg.norm(x - ref) <= 1e-13 * np.linalg.norm(ref)
