@@ -157,3 +157,57 @@ def test_band_and_matrix_free_paths_differ_for_unequal_pml_widths():
     sym = np.array([[2.0, 3.0, 1.0], [2.0, 3.0, 1.0]])
     Hs, idxs = SB.helmholtz_3d_bands(wn, h, sym)
     assert _rel(SB.band_mvp(Hs, idxs, x), mv(*args(sym))[:, 0]) <= 1e-13
+
+
+def _random_band_27(n, seed):
+    """A random complex 27-point band matrix on grid n with unit row norms and no coupling
+    across a face of the grid (test_DoubleKaczmarzSweep.m:26-119 builds its operators so)."""
+    rng = np.random.default_rng(seed)
+    nx, ny, nz = n
+    N = nx * ny * nz
+    H = rng.standard_normal((27, N)) + 1j * rng.standard_normal((27, N))
+    i = np.arange(N) % nx
+    j = (np.arange(N) // nx) % ny
+    k = np.arange(N) // (nx * ny)
+    for t, (dx, dy, dz) in enumerate(SB.OFFS):
+        out = ((i + dx < 0) | (i + dx >= nx) | (j + dy < 0) | (j + dy >= ny) | (k + dz < 0) | (k + dz >= nz))
+        H[t, out] = 0
+    H /= np.sqrt(SB.row_norms_sq(H))[None, :]
+    idx = np.array([dx + nx * dy + nx * ny * dz for dx, dy, dz in SB.OFFS], dtype=np.int64)
+    return H, idx
+
+
+def test_double_sweep_properties_on_random_bands():
+    """The Kaczmarz-sweep properties of test_DoubleKaczmarzSweep.m:125-228 for the compiled
+    sweep_MT_mex on a random row-normalised 27-point band matrix (10 x 11 x 12 grid):
+    I - Q is Hermitian and positive semi-definite (Q x = DSWP(x, 0)), and a double sweep
+    reduces the error of an iterate.  The oracle's sweep agrees with it."""
+    n = (10, 11, 12)
+    H, idx = _random_band_27(n, 3)
+    N = H.shape[1]
+    rn = SB.row_norms_sq(H)
+    sw = M.load_reference("sweep_MT_mex")
+    off = idx.astype(float)
+    rng = np.random.default_rng(4)
+    x = rng.standard_normal((N, 1)) + 1j * rng.standard_normal((N, 1))
+    y = rng.standard_normal((N, 1)) + 1j * rng.standard_normal((N, 1))
+    zero = np.zeros((N, 1), complex)
+    IQ = lambda v: v - sw(H, off, v, np.zeros_like(v), 1.5, rn)
+    lhs = np.vdot(y, IQ(x))
+    rhs = np.vdot(IQ(y), x)
+    assert abs(lhs - rhs) <= 1e-10 * abs(lhs)                                   # Hermitian
+    assert _rel(SB.band_sweep(H, idx, x, zero, 1.5, rn), sw(H, off, x, zero, 1.5, rn)) <= 1e-14
+    E = np.eye(N, dtype=complex)
+    A = E - sw(H, off, E, np.zeros_like(E), 1.5, rn)                            # I - Q, dense
+    assert np.abs(A - A.conj().T).max() <= 1e-10
+    assert np.linalg.eigvalsh((A + A.conj().T) / 2).min() >= -1e-10            # PSD
+    # error reduction: b = A* x*, one double sweep from 0 moves towards x*
+    Bm = np.zeros((N, N), complex)
+    for t in range(27):
+        rows = np.arange(N)
+        cols = rows + idx[t]
+        ok = (cols >= 0) & (cols < N) & (H[t] != 0)
+        Bm[rows[ok], cols[ok]] = H[t, ok]
+    xs = rng.standard_normal((N, 1)) + 1j * rng.standard_normal((N, 1))
+    x1 = sw(H, off, zero, Bm @ xs, 1.5, rn)
+    assert np.linalg.norm(xs - x1) < np.linalg.norm(xs)

@@ -193,3 +193,38 @@ def test_band_path_against_reference_golden(cuda, golden_band):
         assert _rel(y, g[f"{tag}/mvp"]) <= 1e-14
         ys = M.MexFunction(gws["sweep_MT_mex"])(A, o.astype(float), g["X"], g["B"], 1.3, g[f"{tag}/rn"])
         assert _rel(ys, g[f"{tag}/swp"]) <= 1e-12
+
+
+def test_band_double_sweep_properties_on_random_bands(cuda):
+    """test_DoubleKaczmarzSweep.m:125-228 on the GPU band sweep: for a random row-normalised
+    27-point band matrix on a 10 x 11 x 12 grid, I - Q (Q x = DSWP(x, 0)) is Hermitian and
+    positive semi-definite, a double sweep reduces the error of an iterate, and the sweep
+    equals the sequential sweep of sweep_MT_mex (oracle)."""
+    import torch
+    from h3d.band import BandOp
+
+    n = (10, 11, 12)
+    rng = np.random.default_rng(3)
+    nx, ny, nz = n
+    N = nx * ny * nz
+    H = rng.standard_normal((27, N)) + 1j * rng.standard_normal((27, N))
+    i, j, k = np.arange(N) % nx, (np.arange(N) // nx) % ny, np.arange(N) // (nx * ny)
+    for t, (dx, dy, dz) in enumerate(SB.OFFS):
+        H[t, (i + dx < 0) | (i + dx >= nx) | (j + dy < 0) | (j + dy >= ny) | (k + dz < 0) | (k + dz >= nz)] = 0
+    H /= np.sqrt(SB.row_norms_sq(H))[None, :]
+    idx = np.array([dx + nx * dy + nx * ny * dz for dx, dy, dz in SB.OFFS], dtype=np.int64)
+    from h3d import _lib as L
+
+    A = BandOp(torch.as_tensor(H.T.copy(), device=cuda), idx, grid=L.make_grid(n, (1.0, 1.0, 1.0), 0))
+    E = torch.eye(N, dtype=torch.complex128, device=cuda)
+    IQ = (E - A.kacz_sweep(1.5, E)).cpu().numpy().T             # columns: (I - Q) e_j
+    assert np.abs(IQ - IQ.conj().T).max() <= 1e-10                # Hermitian
+    assert np.linalg.eigvalsh((IQ + IQ.conj().T) / 2).min() >= -1e-10
+    x = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    ref = SB.band_sweep(H, idx, x[:, None], np.zeros((N, 1)), 1.5, SB.row_norms_sq(H))[:, 0]
+    got = A.kacz_sweep(1.5, torch.as_tensor(x, device=cuda)).cpu().numpy()
+    assert _rel(got, ref) <= 1e-12
+    xs = torch.as_tensor(x, device=cuda)
+    b = A @ xs
+    x1 = A.kacz_sweep(1.5, torch.zeros_like(xs), b)
+    assert float(torch.linalg.vector_norm(xs - x1)) < float(torch.linalg.vector_norm(xs))
