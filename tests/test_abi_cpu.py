@@ -106,3 +106,20 @@ def test_noalloc_residual_size_check_is_host_only():
     rc = lib.h3d_residual_noalloc(C.byref(small), None, None, None, None, None, None, None, 1, L.FORWARD, None)
     assert rc == L.ERR_BAD_ARG
     assert b"scratch" not in lib.h3d_last_error()
+
+
+def test_bindings_match_header_arity():
+    """Every function include/h3d.h declares is bound in h3d._lib with the same number of
+    parameters (a parameter added to the header but not to the binding would shift every
+    later argument)."""
+    from h3d import _lib
+
+    src = open(os.path.join(ROOT, "include", "h3d.h")).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    decls = re.findall(r"\b(?:int|void|const char \*)\s*\*?\s*(h3d_[a-z0-9_]+)\s*\(([^;]*?)\)\s*;", src, flags=re.S)
+    assert sorted(d[0] for d in decls) == _declared()
+    for name, args in decls:
+        args = args.strip()
+        n = 0 if args in ("", "void") else len(args.split(","))
+        assert name in _lib._SIGS, name
+        assert len(_lib._SIGS[name][1]) == n, (name, n, len(_lib._SIGS[name][1]))
