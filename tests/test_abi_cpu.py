@@ -123,3 +123,20 @@ def test_bindings_match_header_arity():
         n = 0 if args in ("", "void") else len(args.split(","))
         assert name in _lib._SIGS, name
         assert len(_lib._SIGS[name][1]) == n, (name, n, len(_lib._SIGS[name][1]))
+
+
+def test_sinc_kaiser_restatement_against_independent_formula():
+    """The oracle's opSincInterp / kaiser_window / sinc restatement (the checker of the
+    library's source and receiver weights) against the published window evaluated with
+    numpy's own sinc and Bessel I0: w(D) = sinc(D) I0(beta sqrt(1 - (D/r)^2)) / I0(beta) for
+    |D| <= r, 0 beyond, with beta = 6.31 for r = 4 (opSincInterp.m's table)."""
+    from oracle import slim_ref
+
+    r, beta = 4, 6.31
+    for frac in (0.0, 0.3, 0.5, 0.77):
+        xout = np.arange(-6.0, 7.0)                  # unit output spacing
+        got = slim_ref.sinc_interp_matrix([frac], xout, r=r)[:, 0]
+        D = xout - frac
+        want = np.where(np.abs(D) <= r,
+                        np.sinc(D) * np.i0(beta * np.sqrt(np.clip(1 - (D / r) ** 2, 0, None))) / np.i0(beta), 0.0)
+        np.testing.assert_allclose(got, want, rtol=0, atol=1e-14)
