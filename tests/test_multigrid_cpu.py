@@ -110,3 +110,42 @@ def test_fgmres_restart_cycles_match_scipy_gmres():
         yref, _ = gmres(A @ D, b, rtol=1e-30, atol=0.0, restart=m, maxiter=c)
         x, _, _ = MG.fgmres(lambda v: At @ v, bt, None, tol=1e-30, maxit=c, maxinnerit=m, precond=lambda v: Dt @ v)
         assert np.linalg.norm(x.numpy() - D @ yref) <= 1e-12 * np.linalg.norm(D @ yref)
+
+
+def test_library_levels_and_transfers_match_oracle():
+    """h3d.multigrid.build_levels (built on CPU tensors: the grids, PML widths, spacings and
+    wavenumbers of the three levels, and the CSR axis operators of the transfers) against the
+    oracle's construct_multigrid restatement, operator by operator."""
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "slim-release-apps_gb300"))
+    import scipy.sparse as sp
+    from h3d import multigrid as MG
+
+    rng = np.random.default_rng(0)
+    n, h = (17, 15, 13), 25.0
+    z = np.arange(n[2]) * h
+    v = np.broadcast_to(1500 + 1000 * z / z[-1], n).copy() * (1 + 0.05 * rng.standard_normal(n))
+    lv, R, P = MG.build_levels(v, (h, h, h), 6, 4.0, "m/s", device="cpu")
+    levels, Ro, Po = ML.build_levels(v, (h, h, h), 6, 4.0, "m/s")
+    for a, b in zip(lv, levels):
+        assert a.nt == b.nt and a.npml == b.npml and a.dt == b.dt
+        assert np.max(np.abs(a.wn.numpy() - b.wn)) <= 1e-15 * np.max(np.abs(b.wn))
+
+    def sparse(tr):
+        mats = []
+        for op in tr.ops:
+            rp, col, val = op.rowptr.numpy(), op.col.numpy(), op.val.numpy()
+            mats.append(sp.csr_matrix((val, col, rp), shape=(op.n_out, op.n_in)))
+        Ax, Ay, Az = mats
+        return tr.scale * sp.kron(Az, sp.kron(Ay, Ax), format="csr")
+
+    def sparse_o(op):
+        A1, A2, A3 = (sp.csr_matrix(a) for a in op.A)
+        return sp.kron(A3, sp.kron(A2, A1), format="csr")
+
+    for i in range(len(P)):
+        assert abs(sparse(P[i]) - sparse_o(Po[i])).max() <= 1e-14
+        f2c, s = Ro[i]
+        assert abs(sparse(R[i]) - s * sparse_o(f2c)).max() <= 1e-14
