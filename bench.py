@@ -56,7 +56,7 @@ DEFAULT_ORDER = "block8"
 
 # DRAM bytes (read + write) per launch of the dominant kernel, from one ncu capture of the
 # complex64 config-1 solve (python -m h3d.profile --kernel cgmn --config 1 --dtype c64,
-# the capture summarised in profiles/; mean over the 15 launches of one double sweep);
+# mean over the 15 launches of one double sweep);
 # keyed by (order, tuned variant).
 TRAFFIC_PER_LAUNCH = {("block8", 0): 112.6e6}
 
@@ -240,10 +240,14 @@ def run_gpu_arm(args, world, rank):
     from h3d import _lib as L
     from h3d import build, models, solver
 
-    build.build_lib()
-    L.load()
     dev = torch.device("cuda", int(os.environ.get("LOCAL_RANK", "0")))
     torch.cuda.set_device(dev)
+    # one build per node: local rank 0 compiles (the build is also locked and renames its
+    # outputs into place), the other ranks wait at the barrier and then load the library
+    if int(os.environ.get("LOCAL_RANK", "0")) == 0:
+        build.build_lib()
+    _barrier(world)
+    L.load()
     m = models.config1()
     grid = L.make_grid(m.n_total, m.h, m.npml6)
     N = m.N

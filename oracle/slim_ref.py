@@ -293,6 +293,9 @@ def pdefunc(func, v_phys, model, src_pts, src_amp, rec_pts, freqs, Dobs=None, to
     Source amplitudes Q are the per-source scalars ``src_amp`` (Q = diag(src_amp) on a
     source grid that lists the points)."""
     d = model["d"]
+    dt = model.get("dt", d)          # params.dt: model.d unless pdefunopts.helm_dt (PDEfunc.m:88-90)
+    if tuple(dt) != tuple(d):
+        raise NotImplementedError("a Helmholtz grid spacing other than the model's is not restated")
     npml6 = model["npml6"]
     unit = model.get("unit", "m/s")
     n_phys = tuple(model["n"])
@@ -310,7 +313,7 @@ def pdefunc(func, v_phys, model, src_pts, src_amp, rec_pts, freqs, Dobs=None, to
         wn, dwn, _ = param2wavenum(v_pml.reshape(-1, order="F"), fr, unit)           # dh:244,256
         for s in range(nsrc):                                                        # :324
             q = inject(n_total, axes, [src_pts[s]], [w[k] * src_amp[s]])[:, 0]       # :335
-            q = q * np.prod(d) / np.prod(d)                                          # :339
+            q = q * np.prod(d) / np.prod(dt)                                         # :339
             U = divide(g, wn, q, mode=1, tol=tol, maxit=maxit, order=order,
                        nthreads=nthreads)[0]                                         # :347
             dpred = sample(n_total, axes, rec_pts, U)[:, 0]

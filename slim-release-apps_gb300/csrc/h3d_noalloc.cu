@@ -4,7 +4,8 @@
 // only difference is where the scratch lives: one file-scope device array, sized once,
 // instead of buffers from the stream-ordered allocator and the per-grid table cache.
 //
-// Scratch layout (doubles): [PML tables: 2 * 3 * sum_a 3 (n_a + 2)] [partials: 2 * G * nrhs]
+// Scratch layout (doubles): [PML tables: 2 * sum_a 3 (n_a + 2), i.e. three complex tables of
+// n_a + 2 entries per axis] [partials: 2 * G * nrhs]
 // The tables are rewritten on every call; every partial is written by its block before
 // the reduction reads it, so nothing has to start at zero.
 #include <cstring>
@@ -60,9 +61,11 @@ extern "C" int h3d_residual_noalloc(const h3d_grid *g, const double *wn_re, cons
     }
     int rc = check_grid(g);
     if (rc) return rc;
-    // Size check first, before any device call and before the pointers are looked at: a
+    // Size check first, before any launch or copy and before the pointers are looked at: a
     // call with the data pointers left NULL asks only whether the problem fits the scratch,
-    // and can never launch.
+    // and can never launch.  The count of partial sums follows the matvec's z split, which
+    // is chosen from the current device's occupancy (a CUDA query, no launch), so the largest
+    // problem accepted depends on the device.
     size_t tab_entries = 0;
     for (int a = 0; a < 3; ++a) tab_entries += 3 * (size_t)(g->n[a] + 2);
     const size_t tab_doubles = (2 * tab_entries + 31) / 32 * 32;  // keep the partials 256-byte aligned

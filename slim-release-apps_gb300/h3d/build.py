@@ -74,7 +74,42 @@ def _run(cmd, verbose):
     return r
 
 
+class _BuildLock:
+    """An exclusive lock file in the output folder: processes that build at the same time
+    (ranks of one job) take turns, and the second finds the outputs up to date."""
+
+    def __init__(self):
+        os.makedirs(LIBDIR, exist_ok=True)
+        self.path = os.path.join(LIBDIR, ".build.lock")
+        self.f = None
+
+    def __enter__(self):
+        import fcntl
+
+        self.f = open(self.path, "w")
+        fcntl.flock(self.f, fcntl.LOCK_EX)
+        return self
+
+    def __exit__(self, *exc):
+        import fcntl
+
+        fcntl.flock(self.f, fcntl.LOCK_UN)
+        self.f.close()
+
+
+def _compile(cmd_prefix, src, obj, verbose):
+    """Compile to a temporary name, then rename: a reader never sees a half-written object."""
+    tmp = f"{obj}.{os.getpid()}.tmp"
+    _run([*cmd_prefix, "-c", src, "-o", tmp], verbose)
+    os.replace(tmp, obj)
+
+
 def build_lib(verbose: bool = False, force: bool = False, jobs: int | None = None) -> str:
+    with _BuildLock():
+        return _build_lib(verbose, force, jobs)
+
+
+def _build_lib(verbose: bool, force: bool, jobs: int | None) -> str:
     os.makedirs(OBJDIR, exist_ok=True)
     sources = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     headers = sorted(glob.glob(os.path.join(CSRC, "*.cuh"))) + [os.path.join(INCLUDE, "h3d.h")]
@@ -87,17 +122,21 @@ def build_lib(verbose: bool = False, force: bool = False, jobs: int | None = Non
             todo.append((s, o))
     nv = nvcc()
     with cf.ThreadPoolExecutor(max_workers=jobs or min(8, os.cpu_count() or 4)) as ex:
-        futs = [ex.submit(_run, [nv, *NVCC_FLAGS, "-c", s, "-o", o], verbose) for s, o in todo]
+        futs = [ex.submit(_compile, [nv, *NVCC_FLAGS], s, o, verbose) for s, o in todo]
         for f in futs:
             f.result()
     if force or todo or not _newer(LIB, objs):
-        _run([nv, ARCH, "-shared", "-cudart", "shared", "-o", LIB, *objs], verbose)
+        # link to a temporary name and rename: a process that loads the library meanwhile
+        # maps either the old file or the complete new one
+        tmp = f"{LIB}.{os.getpid()}.tmp"
+        _run([nv, ARCH, "-shared", "-cudart", "shared", "-o", tmp, *objs], verbose)
+        os.replace(tmp, LIB)
     return LIB
 
 
 def build_mex(verbose: bool = False, force: bool = False) -> dict:
     """Compile the drop-in gateways against the stub MEX API (oracle/stub) for hosting
-    outside MATLAB; inside MATLAB the same source builds with `mex`."""
+    outside MATLAB; inside MATLAB the same source builds with `mex` and the same -D flags."""
     os.makedirs(MEXDIR, exist_ok=True)
     gw = os.path.join(MEXSRC, "h3d_mex_gateway.c")
     stub_dir = os.path.join(REPO, "oracle", "stub")
@@ -111,16 +150,19 @@ def build_mex(verbose: bool = False, force: bool = False) -> dict:
             continue
         kflag = {"mvp": "-DH3D_GATEWAY_MVP", "swp": "-DH3D_GATEWAY_SWEEP", "bmvp": "-DH3D_GATEWAY_BAND_MVP",
                  "bswp": "-DH3D_GATEWAY_BAND_SWEEP"}[kind]
+        tmp = f"{so}.{os.getpid()}.tmp"
         _run([cc, "-O2", "-std=c11", "-fPIC", "-shared", kflag, *flags, "-I", INCLUDE, "-I",
-              stub_dir, gw, stub_c, "-o", so, "-L", LIBDIR, "-lh3d",
+              stub_dir, gw, stub_c, "-o", tmp, "-L", LIBDIR, "-lh3d",
               "-Wl,-rpath,$ORIGIN/.."], verbose)
+        os.replace(tmp, so)
     return out
 
 
 def build(verbose: bool = False, force: bool = False) -> str:
     lib = build_lib(verbose=verbose, force=force)
     if os.path.exists(os.path.join(MEXSRC, "h3d_mex_gateway.c")):
-        build_mex(verbose=verbose, force=force)
+        with _BuildLock():
+            build_mex(verbose=verbose, force=force)
     return lib
 
 

@@ -81,6 +81,12 @@ class Geometry:
     src_amp: np.ndarray | None = None   # per-source complex amplitude (Q); ones by default
 
     @property
+    def dt(self):
+        """Spacing of the computational grid: params.dt, which PDEfunc.m:88 sets to model.d
+        (a Helmholtz grid coarser or finer than the model, pdefunopts.helm_dt, is not built)."""
+        return tuple(float(x) for x in self.d)
+
+    @property
     def n_total(self):
         p = self.npml6
         return (self.n[0] + p[0] + p[1], self.n[1] + p[2] + p[3], self.n[2] + p[4] + p[5])
@@ -163,7 +169,8 @@ class FWIProblem:
         """Q_k for the listed sources: (len(srcs), N) complex128."""
         ns = len(srcs)
         b = torch.zeros(ns, self.N, dtype=torch.complex128, device=self.dev)
-        scale = self.wavelet[k] * self.src_amp[srcs] * (np.prod(self.geom.d) / np.prod(self.geom.d))
+        # PDEfunc.m:339: wavefield amplitudes independent of the grid spacing
+        scale = self.wavelet[k] * self.src_amp[srcs] * (np.prod(self.geom.d) / np.prod(self.geom.dt))
         sc = torch.as_tensor(np.stack([scale.real, scale.imag], 1), device=self.dev).contiguous()
         base = self.src.base[srcs].contiguous()
         w = self.src.w[srcs].contiguous()
@@ -292,6 +299,25 @@ class FWIProblem:
                 self._grad_accum(dwn, U, V, g)
                 q += 1
         return g
+
+    def objective_pairs(self, v_phys: torch.Tensor, Dobs: torch.Tensor, k: int, srcs):
+        """PDEfunc OBJ restricted to the sources ``srcs`` at frequency index ``k``: (f, g) with g
+        on the physical grid as a (nx, ny, nz) tensor.  Dobs holds every pair's column
+        (src + nsrc * freq, PDEfunc.m:341); the (src, freq) subsets of PDEfunc_dist.m:120-164
+        summed over all pairs give objective()."""
+        srcs = [int(s) for s in srcs]
+        fr = float(self.geom.freqs[k])
+        wn, dwn = self._wavenumbers(v_phys, fr)
+        ml = self._levels(v_phys, fr)
+        U = self._solve(wn, self._sources(k, srcs), 1, ml)
+        cols = [s + self.nsrc * k for s in srcs]
+        dobs = Dobs[:, cols].T.to(self.dev, torch.complex128)
+        r = self._sample(U) - dobs                                   # LS_misfit.m:23
+        f = 0.5 * float(torch.sum(r.real ** 2 + r.imag ** 2))       # LS_misfit.m:24
+        g = torch.zeros(int(np.prod(self.geom.n)), dtype=torch.float64, device=self.dev)
+        V = self._solve(wn, self._spread(r, -1.0), 2, ml)            # H' \ (-Pr' dphi)
+        self._grad_accum(dwn, U, V, g)
+        return f, _unflat(g, self.geom.n)
 
     def objective(self, v_phys: torch.Tensor, Dobs: torch.Tensor):
         """(f, g) as PDEfunc OBJ (no 1/#pairs scaling; misfit_setup applies that)."""

@@ -26,7 +26,10 @@
  *     of being read out of bounds;
  *   - sweep_MT_mex takes the 27 bands of a grid stencil (as helmholtz_3d.m builds them;
  *     the grid is read off the offsets), which the GPU sweeps as parallel hyperplanes;
- *     other band matrices are rejected.
+ *     other band matrices are rejected;
+ *   - Hmvp_MT_mex accepts at most 64 bands and at most 65535 right-hand-side columns per
+ *     call (the reference has neither limit); larger calls are rejected with an error
+ *     instead of being split.
  */
 #include <stddef.h>
 #include <stdio.h>

@@ -18,13 +18,24 @@ What is produced (all from seeded inputs, stored with the inputs):
   regenerated from the seed, so the file stores a checksum of the input, the
   output at 4096 seeded sample indices, its 2-norm and its inner product with a
   seeded probe vector.
+* ``config0_solve.npz`` -- the config-0 forward solve as the reference runs it
+  (linearsolve + CGMN with the compiled ``Helm3d_kacz_sweep_mex``, preconditioned
+  tolerance 1e-6): iteration count, residual history, true residual, and the solution
+  at 4096 seeded indices with its 2-norm and a seeded probe product; beside it the same
+  problem solved to a true residual near 1e-9 by the C oracle ("exact/").
+* ``config3_grad.npz`` -- PDEfunc OBJ on a reduced config-3 problem (the 161x161x81
+  grid, sources 0 and 1 of the 32, all 400 receivers, 6 Hz, squared slowness at the
+  background model, observed data zero), solved in the reference's row order and
+  tolerance: f and the gradient at 4096 seeded indices with its norm and probe product.
 * ``band_small.npz`` -- the band-storage path on a 7x6x8 grid (PML 2): the 27 x N
   band matrix of helmholtz_3d.m (from oracle/slim_band.py, which MATLAB would be
   needed to run directly; pinned to the compiled matrix-free gateways), its adjoint
   bands, and the outputs of the compiled ``Hmvp_MT_mex`` and ``sweep_MT_mex``
   (forward and adjoint bands, 2 right-hand sides).
 
-``python tests/golden/make_golden.py band`` writes only ``band_small.npz``.
+``python tests/golden/make_golden.py band`` writes only ``band_small.npz``;
+``... config0_solve`` (about 80 s) and ``... config3_grad`` (about an hour: four
+single-threaded solves of 2.1 M unknowns, two processes) write one file each.
 """
 from __future__ import annotations
 
@@ -109,6 +120,105 @@ def config0_case(out):
         out[f"{tag}/probe_dot"] = np.array(np.vdot(probe, val))
 
 
+def _samples(val, out, tag, seed=7, count=4096):
+    """Seeded sample indices, the samples, the 2-norm and a seeded probe inner product."""
+    srng = np.random.default_rng(seed)
+    idx = np.sort(srng.choice(val.size, size=min(count, val.size), replace=False))
+    probe = srng.standard_normal(val.size) + 1j * srng.standard_normal(val.size)
+    out[f"{tag}/idx"] = idx
+    out[f"{tag}/samples"] = val[idx]
+    out[f"{tag}/norm"] = np.array(np.linalg.norm(val))
+    out[f"{tag}/probe_dot"] = np.array(np.vdot(probe, val))
+
+
+def config0_solve_case(out):
+    """The config-0 forward solve exactly as the reference runs it: linearsolve.m:148-156
+    (b~ = DSWP(0, b), A = I - DSWP(., 0), w = 1.5, zero start) and the CGMN loop of
+    CGMN.m:48-90 (restated in oracle/slim_ref.cgmn), every double sweep by the compiled
+    reference gateway Helm3d_kacz_sweep_mex (lexicographic order), stopping at the
+    reference's preconditioned residual 1e-6 (CGMN.m:79), at most 2000 iterations."""
+    from h3d import models
+    from oracle import h3d_oracle as O
+    from oracle import slim_ref
+
+    m = models.config0()
+    n = m.n_total
+    N = int(np.prod(n))
+    wn = m.wavenumber()
+    b = m.point_source()
+    hv, nv, npml = np.array(m.h, float), np.array(n, float), m.npml23()
+    swp = M.load_reference("Helm3d_kacz_sweep_mex")
+    mvp = M.load_reference("Helm3dmvp_forw_mex")
+    zero = np.zeros(N, complex)
+    bt = swp(wn, hv, nv, npml, 1.5, zero, b)[:, 0]
+
+    def A(y):
+        return y - swp(wn, hv, nv, npml, 1.5, y, np.zeros_like(y))
+
+    x, hst = slim_ref.cgmn(A, bt, zero.copy(), tol=1e-6, maxit=2000)
+    r = b - mvp(wn, hv, nv, npml, x, float(os.cpu_count()))[:, 0]
+    out["n"] = np.array(n, float)
+    out["wn_checksum"] = np.array([np.sum(wn), np.linalg.norm(wn), wn.min(), wn.max()])
+    out["src_index"] = np.array(int(np.flatnonzero(b)[0]))
+    out["iters"] = np.array(len(hst) - 1)
+    out["hist"] = hst
+    out["rel_res_true"] = np.array(np.linalg.norm(r) / np.linalg.norm(b))
+    _samples(x, out, "u")
+    # the same problem solved to a true residual near 1e-9 (C oracle, COLOUR27 row order,
+    # preconditioned tolerance 1e-10): the FP64 reference the errors of faster solves are
+    # stated against
+    g = O.make_grid(n, m.h, m.npml6)
+    xe, he = slim_ref.linearsolve_cgmn(g, wn, b, tol=1e-10, maxit=20000, order=O.ORDER_COLOUR27,
+                                       nthreads=os.cpu_count())
+    out["exact/iters"] = np.array(len(he) - 1)
+    out["exact/rel_res_true"] = np.array(slim_ref.true_residual(g, wn, b, xe))
+    _samples(xe, out, "exact")
+
+
+def _config3_reduced():
+    """The reduced config-3 gradient problem: sources 0 and 1 of the 32, all 400 receivers,
+    6 Hz only, gradient w.r.t. squared slowness at the background model, observed data 0."""
+    from h3d import models
+
+    m = models.config3()
+    meta = m.meta
+    model = {"o": (0.0, 0.0, 0.0), "d": m.h, "n": m.n_phys, "npml6": m.npml6, "unit": "s2/m2",
+             "f0": meta["f0"], "t0": 0.0}
+    m0 = (meta["v0"] ** -2.0).reshape(-1, order="F")
+    return model, m0, meta["src_xyz"][:2], meta["rec_xyz"], np.array([6.0])
+
+
+def _config3_worker(s):
+    from oracle import h3d_oracle as O
+    from oracle import slim_ref
+
+    model, m0, src, rec, freqs = _config3_reduced()
+    Dobs = np.zeros((len(rec), 1), complex)
+    f, g = slim_ref.pdefunc("obj", m0, model, src[s:s + 1], np.ones(1), rec, freqs, Dobs=Dobs,
+                            tol=1e-6, maxit=10000, order=O.ORDER_LEX, nthreads=1)
+    return f, g
+
+
+def config3_grad_case(out):
+    """PDEfunc OBJ (oracle/slim_ref.pdefunc over the C oracle, whose lexicographic sweep equals
+    the compiled reference gateway bit for bit) on the reduced config-3 problem of
+    _config3_reduced(), one source per process; the reference's own solver settings
+    (CGMN, tol 1e-6 on the preconditioned residual, one source at a time, PDEfunc.m:157)."""
+    import multiprocessing as mp
+
+    model, m0, src, rec, freqs = _config3_reduced()
+    with mp.get_context("spawn").Pool(len(src)) as pool:
+        res = pool.map(_config3_worker, range(len(src)))
+    f = sum(r[0] for r in res)
+    g = np.sum([r[1] for r in res], axis=0)
+    out["f"] = np.array(f)
+    out["f_per_source"] = np.array([r[0] for r in res])
+    out["n_phys"] = np.array(model["n"], float)
+    out["freqs"] = freqs
+    out["m0_checksum"] = np.array([np.sum(m0), np.linalg.norm(m0)])
+    _samples(g, out, "g")
+
+
 def band_case(out):
     from oracle import slim_band as SB
 
@@ -137,6 +247,18 @@ def band_case(out):
 def main():
     if not M.reference_available():
         raise SystemExit("reference gateways missing: run `make -C oracle ref` first")
+    if sys.argv[1:] == ["config0_solve"]:
+        c0s: dict = {}
+        config0_solve_case(c0s)
+        np.savez_compressed(os.path.join(HERE, "config0_solve.npz"), **c0s)
+        print("wrote config0_solve.npz: iterations", int(c0s["iters"]))
+        return
+    if sys.argv[1:] == ["config3_grad"]:
+        c3: dict = {}
+        config3_grad_case(c3)
+        np.savez_compressed(os.path.join(HERE, "config3_grad.npz"), **c3)
+        print("wrote config3_grad.npz: f", float(c3["f"]))
+        return
     band: dict = {}
     band_case(band)
     np.savez_compressed(os.path.join(HERE, "band_small.npz"), **band)

@@ -92,8 +92,9 @@ def test_sinc_weights_host_match_oracle():
 
 
 def test_noalloc_residual_size_check_is_host_only():
-    """h3d_residual_noalloc refuses a problem beyond its fixed scratch before any device
-    call and before it looks at the data pointers (left NULL here)."""
+    """h3d_residual_noalloc refuses a problem beyond its fixed scratch before any launch or
+    copy and before it looks at the data pointers (left NULL here); on a host without a GPU
+    the occupancy query behind the z split fails and the default split is used."""
     from h3d import _lib as L
 
     lib = L.load()
