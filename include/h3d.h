@@ -23,7 +23,9 @@
  *                      preconditioner (tools/solvers/Krylov/linearsolve.m:148-168,
  *                      CGMN.m:36-94, opAbstractMatrix.m:117-125)
  *   h3d_solve_batch    many (problem, right-hand side) solves of uneven size in one launch
- *                      sequence (the (src,freq) loop of PDEfunc.m:254-347 batched)
+ *                      sequence (the (src,freq) loop of PDEfunc.m:254-347 batched: one CGMN
+ *                      iteration over every column, one BLOCK8 launch per block parity over
+ *                      every problem)
  *   h3d_grad_accum     T_adj(z,u) = conj(u).*(dH'*z) summed over sources and cropped to the
  *                      physical grid (discrete_helmholtz.m:288, PDEfunc.m:386,394)
  *   h3d_src_inject,    sinc-Kaiser source injection Ps and receiver sampling Pr
@@ -168,7 +170,9 @@ int h3d_mvp(const h3d_grid *g, const void *wn_re, const void *wn_im, const void 
  * (NULL or 0 = default).  COLOUR27 and BLOCK8 with 12x12x12 blocks run on stored row
  * coefficients (about 27 N complex values of temporary device memory) whenever they fit;
  * block[0] == -1 selects the kernels that form the coefficients themselves (COLOUR27: the
- * shared-memory tile kernel; BLOCK8: 12x12x12 blocks). */
+ * shared-memory tile kernel; BLOCK8: 12x12x12 blocks).  BLOCK8 on stored coefficients reads
+ * the kernel's status word back (H3D_ERR_TIMEOUT if a bounded wait expired), so that call
+ * synchronises the stream. */
 int h3d_kacz_sweep(const h3d_grid *g, const void *wn_re, const void *wn_im, double w, void *x,
                    const void *b, int nrhs, int mode, int order, const int32_t *block, int dtype,
                    void *stream);
@@ -184,7 +188,10 @@ int h3d_residual(const h3d_grid *g, const double *wn_re, const double *wn_im, co
  * would fail there or break the caller's accounting).  No counterpart in the reference.
  * All scratch (the PML tables and the per-block partial sums) lives in one fixed device
  * array of H3D_NOALLOC_SCRATCH_BYTES that every GPU loading the library holds until the
- * process exits; grids and nrhs needing more are rejected with H3D_ERR_BAD_ARG.  The
+ * process exits; grids and nrhs needing more are rejected with H3D_ERR_BAD_ARG, before any
+ * launch.  The scratch holds one partial sum per 32x8-column block, z chunk and right-hand
+ * side, and the z split follows the current device's occupancy, so the largest problem
+ * accepted depends on the device.  The
  * first call on a device looks up that array's address (once per device, with the device
  * current); make the first call before any stream capture.  Every call reuses the same
  * array, so calls that overlap on the GPU (other streams, other threads) race: serialise
@@ -193,6 +200,16 @@ int h3d_residual(const h3d_grid *g, const double *wn_re, const double *wn_im, co
 int h3d_residual_noalloc(const h3d_grid *g, const double *wn_re, const double *wn_im,
                          const void *b, const void *x, void *r, double *rr2, double *bb2,
                          int nrhs, int mode, void *stream);
+
+/* ---- diagnostics ------------------------------------------------------------------------ */
+/* Checks the bounded waits of the BLOCK8 sweep kernel on this GPU (no counterpart in the
+ * reference).  Runs one double sweep on an internal 24^3 problem in which the kernel's first
+ * colour step announces a coefficient copy on its mbarrier but never issues it, with every
+ * wait limited to limit_ms (0 < limit_ms <= 1000): each CTA gives up after the limit, records
+ * the expired wait in the sweep's status word and returns.  Returns H3D_ERR_TIMEOUT when that
+ * status came back (the expected result; the context stays usable), H3D_OK if no wait
+ * expired, or another status if the call itself failed.  Synchronous. */
+int h3d_check_wait_timeout(double limit_ms);
 
 /* ---- MATLAB-layout host entry points (what the drop-in MEX gateway calls) ----------- */
 /* Arguments exactly as the reference gateways receive them: wn (N, re/im planes; im may
@@ -217,7 +234,12 @@ int h3d_solve(const h3d_grid *g, const double *wn_re, const double *wn_im, const
               void *u, int nrhs, int mode, const h3d_solve_opts *opts, h3d_solve_info *info,
               double *res_hist, int res_hist_len, void *stream);
 
-/* Solve every problem of the table; infos (host, nprob entries) may be NULL. */
+/* Solve every problem of the table; infos (host, nprob entries) may be NULL.  With the BLOCK8
+ * order (12^3 blocks) and room for every problem's stored coefficients in device memory, all
+ * problems run as one batched solve: their columns iterate together (each with its own
+ * convergence mask), and every sweep launch covers all problems; problems may differ in grid,
+ * PML, wavenumber and mode.  Otherwise the problems are solved one after another.  The wall
+ * time in each info is that of the whole call. */
 int h3d_solve_batch(const h3d_problem *probs, int nprob, const h3d_solve_opts *opts,
                     h3d_solve_info *infos, void *stream);
 

@@ -2,7 +2,9 @@
 // device-pointer form and in the MATLAB host layout used by the drop-in MEX gateway.
 #include <cmath>
 #include <cstring>
+#include <vector>
 
+#include "h3d_b8.cuh"
 #include "h3d_internal.cuh"
 #include "h3d_kernels.cuh"
 #include "h3d_vec.cuh"
@@ -33,13 +35,29 @@ static int kacz_sweep_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs,
     }
     const bool blk12 = !block || block[0] == 0 || (block[0] == 12 && block[1] == 12 && block[2] == 12);
     if (order == H3D_ORDER_BLOCK8 && blk12) {
-        DevBuf cb;
-        if (cb.alloc(sizeof(cplx<T>) * block8_coef_count(op.nx, op.ny, op.nz), st) == H3D_OK) {
-            int rc = store_block8_coefs<T>(op, adj, cb.as<cplx<T>>(), st);
-            if (!rc) rc = launch_sweep<T>(op, x, b, nrhs, w, adj, order, block, nullptr, st, nullptr, -1, cb.as<cplx<T>>());
-            return rc;
+        // the batched BLOCK8 kernel on one problem (stored coefficients, bulk-copied slabs);
+        // its status word is read back, so this call synchronises the stream
+        B8Batch<T> batch;
+        batch.add(op, adj, 0, 0, nrhs);
+        int rc = batch.setup(st);
+        if (rc == H3D_ERR_NO_MEMORY) {
+            (void)cudaGetLastError();  // out of memory is not sticky: fall back below
+        } else {
+            if (rc) return rc;
+            const bool fp64 = sizeof(T) == 8;
+            int c = 0;  // the largest right-hand-side group the columns fill
+            for (int k = 1; k < b8_num_cfgs(fp64); ++k)
+                if (b8_cfg(fp64, k).r <= nrhs) c = k;
+            if ((rc = batch.configure(c, st)) || (rc = batch.dsweep(x, b, w, nullptr, st))) return rc;
+            int status = 0;
+            H3D_CUDA_TRY(cudaMemcpyAsync(&status, batch.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+            H3D_CUDA_TRY(cudaStreamSynchronize(st));
+            if (status) {
+                set_error("a bounded wait of the BLOCK8 sweep expired (device status %d)", status);
+                return H3D_ERR_TIMEOUT;
+            }
+            return H3D_OK;
         }
-        (void)cudaGetLastError();
     }
     return launch_sweep<T>(op, x, b, nrhs, w, adj, order, block, nullptr, st);
 }
@@ -257,6 +275,52 @@ int h3d_mex_kacz_sweep(const double *wn_re, const double *wn_im, const double *h
     if (rc) return rc;
     if (e != cudaSuccess) return cuda_fail(e, "h3d_mex_kacz_sweep");
     return H3D_OK;
+}
+
+int h3d_check_wait_timeout(double limit_ms)
+{
+    if (!(limit_ms > 0) || limit_ms > 1000) {
+        set_error("h3d_check_wait_timeout: limit_ms must lie in (0, 1000]");
+        return H3D_ERR_BAD_ARG;
+    }
+    // An internal 24 x 24 x 24 problem (PML 6, h 20 m, 5 Hz, wavenumber of 2000 m/s): every
+    // block has PML rows, so every step of the BLOCK8 kernel waits on a bulk copy.
+    const int n = 24;
+    const long long N = (long long)n * n * n;
+    h3d_grid g{};
+    for (int a = 0; a < 3; ++a) {
+        g.n[a] = n;
+        g.h[a] = 20.0;
+    }
+    for (int a = 0; a < 6; ++a) g.npml[a] = 6;
+    cudaStream_t st = nullptr;
+    H3D_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+    int status = 0;
+    int rc = [&]() -> int {
+        DevBuf wn, x;
+        int r;
+        if ((r = wn.alloc(sizeof(float) * (size_t)N, st)) || (r = x.alloc(sizeof(cplx<float>) * (size_t)N, st))) return r;
+        const double k2 = std::pow(2.0 * M_PI * 5.0 / 2000.0, 2);
+        std::vector<float> h((size_t)N, (float)k2);
+        H3D_CUDA_TRY(cudaMemcpyAsync(wn.p, h.data(), sizeof(float) * (size_t)N, cudaMemcpyHostToDevice, st));
+        H3D_CUDA_TRY(cudaMemsetAsync(x.p, 0, sizeof(cplx<float>) * (size_t)N, st));
+        Op<float> op;
+        if ((r = make_op_f32(&g, wn.as<float>(), nullptr, &op))) return r;
+        B8Batch<float> batch;
+        batch.add(op, false, 0, 0, 1);
+        if ((r = batch.setup(st)) || (r = batch.configure(0, st))) return r;
+        batch.wait_limit_ns = (unsigned long long)(limit_ms * 1e6);
+        if ((r = batch.dsweep(x.as<cplx<float>>(), nullptr, 1.5f, nullptr, st, 1))) return r;
+        H3D_CUDA_TRY(cudaMemcpyAsync(&status, batch.err, sizeof(int), cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaStreamSynchronize(st));
+        return H3D_OK;
+    }();
+    cudaError_t e = cudaStreamSynchronize(st);
+    cudaStreamDestroy(st);
+    if (rc) return rc;
+    if (e != cudaSuccess) return cuda_fail(e, "cudaStreamSynchronize");
+    if (status) set_error("the BLOCK8 sweep reported an expired wait (status %d)", status);
+    return status;
 }
 
 }  // extern "C"

@@ -64,11 +64,11 @@ __device__ __forceinline__ double2 sum_partials(const double *part, int G, int s
 
 template <typename T>
 __global__ void k_init(const cplx<T> *__restrict__ bt, cplx<T> *__restrict__ x,
-                       cplx<T> *__restrict__ r, cplx<T> *__restrict__ p, long long N, double *part,
+                       cplx<T> *__restrict__ r, cplx<T> *__restrict__ p, ColMap cm, double *part,
                        int G)
 {
     const int s = blockIdx.y;
-    const long long off = (long long)s * N;
+    const long long off = cm.o(s), N = cm.n(s);
     double acc = 0.0;
     for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < N;
          q += (long long)G * blockDim.x) {
@@ -112,7 +112,7 @@ int cg_init(const cplx<T> *bt, cplx<T> *x, cplx<T> *r, cplx<T> *p, long long N, 
             cudaStream_t st)
 {
     (void)maxit;
-    k_init<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(bt, x, r, p, N, s.part, s.G);
+    k_init<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(bt, x, r, p, ColMap{s.coloff, s.collen, N}, s.part, s.G);
     k_init_state<<<nrhs, kVecThreads, 0, st>>>(s, bnorm2_orig, zero_tol2, nrhs);
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;
@@ -120,13 +120,14 @@ int cg_init(const cplx<T> *bt, cplx<T> *x, cplx<T> *r, cplx<T> *p, long long N, 
 
 // Ap = p - y (written over y), partial <p, Ap> (complex).
 template <typename T>
-__global__ void k_ap_dot(const cplx<T> *__restrict__ p, cplx<T> *__restrict__ y, long long N,
+__global__ void k_ap_dot(const cplx<T> *__restrict__ p, cplx<T> *__restrict__ y, ColMap cm,
                          const int *__restrict__ active, double *part, int G)
 {
     const int s = blockIdx.y;
     if (!active[s]) return;
-    const cplx<T> *ps = p + (long long)s * N;
-    cplx<T> *ys = y + (long long)s * N;
+    const long long N = cm.n(s);
+    const cplx<T> *ps = p + cm.o(s);
+    cplx<T> *ys = y + cm.o(s);
     double are = 0.0, aim = 0.0;
     auto body = [&](const cplx<T> pv, const cplx<T> yv, long long q) {
         const cplx<T> ap = pv - yv;
@@ -186,7 +187,8 @@ template <typename T>
 int cg_ap_dot(const cplx<T> *p, cplx<T> *y, long long N, int nrhs, const CgState &s,
               cudaStream_t st)
 {
-    k_ap_dot<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(p, y, N, s.active, s.part, s.G);
+    k_ap_dot<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(p, y, ColMap{s.coloff, s.collen, N}, s.active,
+                                                         s.part, s.G);
     k_alpha<<<nrhs, kVecThreads, 0, st>>>(s);
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;
@@ -196,12 +198,12 @@ int cg_ap_dot(const cplx<T> *p, cplx<T> *y, long long N, int nrhs, const CgState
 template <typename T>
 __global__ void k_update_xr(cplx<T> *__restrict__ x, cplx<T> *__restrict__ r,
                             const cplx<T> *__restrict__ p, const cplx<T> *__restrict__ ap,
-                            long long N, const int *__restrict__ active,
+                            ColMap cm, const int *__restrict__ active,
                             const double *__restrict__ alpha, double *part, int G)
 {
     const int s = blockIdx.y;
     if (!active[s]) return;
-    const long long off = (long long)s * N;
+    const long long off = cm.o(s), N = cm.n(s);
     cplx<T> *xs = x + off, *rs = r + off;
     const cplx<T> *ps = p + off, *as = ap + off;
     const cplx<T> a = mk<T>((T)alpha[2 * s], (T)alpha[2 * s + 1]);
@@ -272,8 +274,8 @@ template <typename T>
 int cg_update_xr(cplx<T> *x, cplx<T> *r, const cplx<T> *p, const cplx<T> *ap, long long N,
                  int nrhs, const CgState &s, int maxit, cudaStream_t st)
 {
-    k_update_xr<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(x, r, p, ap, N, s.active, s.alpha,
-                                                            s.part, s.G);
+    k_update_xr<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(x, r, p, ap, ColMap{s.coloff, s.collen, N},
+                                                            s.active, s.alpha, s.part, s.G);
     k_beta<<<nrhs, kVecThreads, 0, st>>>(s, maxit);
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;
@@ -282,12 +284,12 @@ int cg_update_xr(cplx<T> *x, cplx<T> *r, const cplx<T> *p, const cplx<T> *ap, lo
 // p = r + beta p; y = p (the copy the next sweep works on).
 template <typename T>
 __global__ void k_update_p(cplx<T> *__restrict__ p, const cplx<T> *__restrict__ r,
-                           cplx<T> *__restrict__ y, long long N, const int *__restrict__ upd,
+                           cplx<T> *__restrict__ y, ColMap cm, const int *__restrict__ upd,
                            const double *__restrict__ beta, int G)
 {
     const int s = blockIdx.y;
     if (!upd[s]) return;
-    const long long off = (long long)s * N;
+    const long long off = cm.o(s), N = cm.n(s);
     cplx<T> *ps = p + off, *ys = y + off;
     const cplx<T> *rs = r + off;
     const T b = (T)beta[s];
@@ -318,7 +320,8 @@ template <typename T>
 int cg_update_p(cplx<T> *p, const cplx<T> *r, cplx<T> *y, long long N, int nrhs,
                 const CgState &s, cudaStream_t st)
 {
-    k_update_p<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(p, r, y, N, s.upd, s.beta, s.G);
+    k_update_p<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(p, r, y, ColMap{s.coloff, s.collen, N}, s.upd,
+                                                           s.beta, s.G);
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;
 }
@@ -328,12 +331,12 @@ int cg_update_p(cplx<T> *p, const cplx<T> *r, cplx<T> *y, long long N, int nrhs,
 template <typename T>
 __global__ void k_cr_update_xr(cplx<T> *__restrict__ x, cplx<T> *__restrict__ r,
                                const cplx<T> *__restrict__ p, const cplx<T> *__restrict__ ap,
-                               cplx<T> *__restrict__ y, long long N, const int *__restrict__ active,
+                               cplx<T> *__restrict__ y, ColMap cm, const int *__restrict__ active,
                                const double *__restrict__ gamma, double *part, int G)
 {
     const int s = blockIdx.y;
     if (!active[s]) return;
-    const long long off = (long long)s * N;
+    const long long off = cm.o(s), N = cm.n(s);
     cplx<T> *xs = x + off, *rs = r + off, *ys = y + off;
     const cplx<T> *ps = p + off, *as = ap + off;
     const cplx<T> g = mk<T>((T)gamma[2 * s], (T)gamma[2 * s + 1]);
@@ -372,8 +375,8 @@ template <typename T>
 int cr_update_xr(cplx<T> *x, cplx<T> *r, const cplx<T> *p, const cplx<T> *ap, cplx<T> *y,
                  long long N, int nrhs, const CgState &s, int maxit, cudaStream_t st)
 {
-    k_cr_update_xr<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(x, r, p, ap, y, N, s.active, s.alpha,
-                                                               s.part, s.G);
+    k_cr_update_xr<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(x, r, p, ap, y, ColMap{s.coloff, s.collen, N},
+                                                               s.active, s.alpha, s.part, s.G);
     k_beta<<<nrhs, kVecThreads, 0, st>>>(s, maxit);  // ||r||, iteration count, stop test
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;
@@ -383,7 +386,8 @@ int cr_update_xr(cplx<T> *x, cplx<T> *r, const cplx<T> *p, const cplx<T> *ap, cp
 template <typename T>
 int cr_ar_dot(const cplx<T> *r, cplx<T> *y, long long N, int nrhs, const CgState &s, cudaStream_t st)
 {
-    k_ap_dot<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(r, y, N, s.active, s.part, s.G);
+    k_ap_dot<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(r, y, ColMap{s.coloff, s.collen, N}, s.active,
+                                                         s.part, s.G);
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;
 }
@@ -416,13 +420,13 @@ __global__ void k_cr_beta(CgState st, int first)
 // p = r + beta p; Ap = Ar + beta Ap; partial ||Ap||^2 (CRMN.m:103-105).
 template <typename T>
 __global__ void k_cr_update_p(cplx<T> *__restrict__ p, cplx<T> *__restrict__ ap,
-                              const cplx<T> *__restrict__ r, const cplx<T> *__restrict__ ar, long long N,
+                              const cplx<T> *__restrict__ r, const cplx<T> *__restrict__ ar, ColMap cm,
                               const int *__restrict__ active, const double *__restrict__ cbeta,
                               double *part, int G)
 {
     const int s = blockIdx.y;
     if (!active[s]) return;
-    const long long off = (long long)s * N;
+    const long long off = cm.o(s), N = cm.n(s);
     cplx<T> *ps = p + off, *aps = ap + off;
     const cplx<T> *rs = r + off, *ars = ar + off;
     const cplx<T> b = mk<T>((T)cbeta[2 * s], (T)cbeta[2 * s + 1]);
@@ -479,8 +483,8 @@ int cr_update_p(cplx<T> *p, cplx<T> *ap, const cplx<T> *r, const cplx<T> *ar, lo
                 const CgState &s, bool first, cudaStream_t st)
 {
     k_cr_beta<<<nrhs, kVecThreads, 0, st>>>(s, first ? 1 : 0);
-    k_cr_update_p<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(p, ap, r, ar, N, s.active, s.cbeta,
-                                                              s.part, s.G);
+    k_cr_update_p<T><<<dim3(s.G, nrhs), kVecThreads, 0, st>>>(p, ap, r, ar, ColMap{s.coloff, s.collen, N},
+                                                              s.active, s.cbeta, s.part, s.G);
     k_cr_gamma<<<nrhs, kVecThreads, 0, st>>>(s);
     H3D_CUDA_TRY(cudaGetLastError());
     return H3D_OK;

@@ -23,9 +23,20 @@ struct CgState {
     int *status;      // 0 ok, H3D_ERR_NONFINITE on NaN/Inf
     double *part;     // reduction partials: nrhs x G x 2
     int G;            // reduction blocks per RHS
+    // Column map of a batch of problems of uneven size (null: column s of N elements at s N):
+    // column s spans [coloff[s], coloff[s] + collen[s]) of every vector.
+    const long long *coloff = nullptr, *collen = nullptr;
     // CRMN only (null for CGMN): complex <r, A r> (re, im) pairs, complex beta pairs,
     // ||A p||^2; alpha holds gamma.
     double *rar = nullptr, *cbeta = nullptr, *nap2 = nullptr;
+};
+
+// Where column s of the CG vectors lives (see CgState::coloff).
+struct ColMap {
+    const long long *off, *len;
+    long long N;
+    __device__ __forceinline__ long long o(int s) const { return off ? off[s] : (long long)s * N; }
+    __device__ __forceinline__ long long n(int s) const { return len ? len[s] : N; }
 };
 
 constexpr int kVecThreads = 256;

@@ -8,7 +8,15 @@
 // Iterations are recorded once into a CUDA graph (check_every iterations per graph) and
 // replayed; per-RHS masks freeze converged right-hand sides on the device, and the host
 // only reads the mask every check_every iterations.
+//
+// With the BLOCK8 order (12^3 blocks, stored coefficients in device memory) one CGMN
+// instance iterates every column of a table of problems at once: the problems' columns
+// sit one after another in each CG vector (problem-major), the vector kernels follow a
+// per-column offset and length, and one batched sweep launch per block parity covers all
+// problems (h3d_b8batch.cu).  Problems may differ in grid, PML, wavenumber and mode.
+#include <algorithm>
 #include <chrono>
+#include <type_traits>
 #include <map>
 #include <mutex>
 #include <tuple>
@@ -17,6 +25,7 @@
 #include <cstring>
 #include <vector>
 
+#include "h3d_b8.cuh"
 #include "h3d_internal.cuh"
 #include "h3d_kernels.cuh"
 #include "h3d_krylov.cuh"
@@ -79,8 +88,12 @@ static void tune_store(const TuneKey &k, int shape)
 template <typename T>
 struct CgRun {
     Op<T> op{};
-    long long N = 0;
-    int nrhs = 0;
+    long long N = 0;   // column length (batched: the longest column)
+    long long L = 0;   // elements of each CG vector (N nrhs, or the batch's total)
+    int nrhs = 0;      // columns
+    B8Batch<T> *b8 = nullptr;           // batched BLOCK8 sweeps (null: sweeps of op)
+    std::vector<long long> coloff, collen;  // batched: column map (host copy)
+    bool b8_tuned = false;
     bool adj = false;
     T w = T(1.5);
     int order = H3D_ORDER_COLOUR27;
@@ -94,7 +107,7 @@ struct CgRun {
     int shape = -1;      // COLOUR27 tile shape (num_tile_shapes(): stored coefficients), BLOCK cfg
     cplx<T> *coef = nullptr;  // stored row coefficients (COLOUR27: colour-major 27 N; BLOCK8: 12^3 block layout)
     CgState s{};
-    DevBuf vecs, scal, ints, parts, norms, coefs;
+    DevBuf vecs, scal, ints, parts, norms, coefs, cmap;
     cudaGraphExec_t exec = nullptr;
     int graph_iters = 0;
     // Timing of the last double sweep of every replayed block: two timing events recorded
@@ -129,16 +142,26 @@ struct CgRun {
 
     int alloc(cudaStream_t st)
     {
-        const size_t vb = sizeof(cplx<T>) * (size_t)N * nrhs;
+        if (!b8) L = N * nrhs;
+        const size_t vb = sizeof(cplx<T>) * (size_t)L;
         int rc;
         const bool cr = method == H3D_METHOD_CRMN;
         if ((rc = vecs.alloc((cr ? 5 : 4) * vb, st))) return rc;
         x = vecs.as<cplx<T>>();
-        r = x + N * nrhs;
-        p = r + N * nrhs;
-        y = p + N * nrhs;
-        ap = cr ? y + N * nrhs : nullptr;
+        r = x + L;
+        p = r + L;
+        y = p + L;
+        ap = cr ? y + L : nullptr;
         s.G = reduction_blocks(N);
+        if (b8) {
+            if ((rc = cmap.alloc(sizeof(long long) * 2 * (size_t)nrhs, st))) return rc;
+            std::vector<long long> h(coloff);
+            h.insert(h.end(), collen.begin(), collen.end());
+            // pageable source: staged before the call returns
+            H3D_CUDA_TRY(cudaMemcpyAsync(cmap.p, h.data(), sizeof(long long) * h.size(), cudaMemcpyHostToDevice, st));
+            s.coloff = cmap.as<long long>();
+            s.collen = s.coloff + nrhs;
+        }
         if ((rc = scal.alloc(sizeof(double) * (size_t)nrhs * (cr ? 12 : 7), st))) return rc;
         double *d = scal.as<double>();
         s.rr = d;
@@ -160,6 +183,7 @@ struct CgRun {
         s.status = q + 3 * nrhs;
         if ((rc = parts.alloc(sizeof(double) * 2 * (size_t)s.G * nrhs, st))) return rc;
         s.part = parts.as<double>();
+        if (b8) return H3D_OK;  // the batch holds its own coefficients and row norms
         if (order != H3D_ORDER_LEX) {
             if ((rc = norms.alloc(sizeof(T) * (size_t)N, st))) return rc;
             rinv = norms.as<T>();
@@ -191,8 +215,16 @@ struct CgRun {
         return H3D_OK;
     }
 
+    // One double sweep of v with right-hand side b (null = 0) over the active columns.
+    int sweep(cplx<T> *v, const cplx<T> *b, const int *act, cudaStream_t st)
+    {
+        if (b8) return b8->dsweep(v, b, w, act, st);
+        return launch_sweep<T>(op, v, b, nrhs, w, adj, order, block, act, st, rinv, shape, cf());
+    }
+
     int sweep_launches() const
     {
+        if (b8) return b8->launches();
         if (order == H3D_ORDER_LEX) return 2 * ((op.nx - 1) + 3 * (op.ny - 1) + 9 * (op.nz - 1) + 1);
         if (order == H3D_ORDER_BLOCK) {
             int32_t bd[3] = {block[0] > 0 ? block[0] : 8, block[1] > 0 ? block[1] : 8, block[2] > 0 ? block[2] : 8};
@@ -218,6 +250,14 @@ struct CgRun {
     // and keep the fastest; decisions are cached per (grid, precision, mode, nrhs).
     int tune(cudaStream_t st)
     {
+        if (b8) {
+            if (b8_tuned) return H3D_OK;
+            b8_tuned = true;
+            const int rc = b8->tune(y, L, st);
+            launches += 5LL * sweep_launches();  // upper bound: at most the configurations the columns fill
+            shape = b8->cfg;
+            return rc;
+        }
         if (order == H3D_ORDER_LEX || shape >= 0) return H3D_OK;
         if (order != H3D_ORDER_COLOUR27 && block[0] > 0) return H3D_OK;  // explicit block size
         const TuneKey key{op.nx, op.ny, op.nz, (int)sizeof(T) + 100 * order, adj ? 1 : 0, op.wni ? 1 : 0, nrhs};
@@ -310,8 +350,8 @@ struct CgRun {
     {
         int rc;
         if ((rc = tune(st))) return rc;
-        if ((rc = zero_vec<T>(y, N, nrhs, st))) return rc;
-        if ((rc = launch_sweep<T>(op, y, b, nrhs, w, adj, order, block, nullptr, st, rinv, shape, cf()))) return rc;
+        if ((rc = zero_vec<T>(y, L, 1, st))) return rc;
+        if ((rc = sweep(y, b, nullptr, st))) return rc;
         launches += sweep_launches() + 2;
         if ((rc = cg_init<T>(y, x, r, p, N, nrhs, s, bnorm2_orig, zero_tol2, maxit, st))) return rc;
         if (method != H3D_METHOD_CRMN) return H3D_OK;
@@ -319,8 +359,8 @@ struct CgRun {
         // Ar = A r, p = r, Ap = Ar, gamma; then the first x, r update and stop test
         // (CRMN.m:79-92).  Every later iteration starts at Ar = A r (CRMN.m:94), so a
         // right-hand side stopped by the test resumes exactly where CRMN.m would continue.
-        if ((rc = zero_vec<T>(ap, N, nrhs, st))) return rc;
-        if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st, rinv, shape, cf()))) return rc;
+        if ((rc = zero_vec<T>(ap, L, 1, st))) return rc;
+        if ((rc = sweep(y, nullptr, s.active, st))) return rc;
         if ((rc = cr_ar_dot<T>(r, y, N, nrhs, s, st))) return rc;
         if ((rc = cr_update_p<T>(p, ap, r, y, N, nrhs, s, true, st))) return rc;
         if ((rc = cr_update_xr<T>(x, r, p, ap, y, N, nrhs, s, maxit, st))) return rc;
@@ -335,14 +375,14 @@ struct CgRun {
             // CRMN.m:94-105 then 73-92: Ar = A r (y = r on entry), rAr, beta, p, Ap, ||Ap||,
             // gamma; x, r, y = r, the stop test
             if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev0, st, cudaEventRecordExternal));
-            if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st, rinv, shape, cf()))) return rc;
+            if ((rc = sweep(y, nullptr, s.active, st))) return rc;
             if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev1, st, cudaEventRecordExternal));
             if ((rc = cr_ar_dot<T>(r, y, N, nrhs, s, st))) return rc;
             if ((rc = cr_update_p<T>(p, ap, r, y, N, nrhs, s, false, st))) return rc;
             return cr_update_xr<T>(x, r, p, ap, y, N, nrhs, s, maxit, st);
         }
         if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev0, st, cudaEventRecordExternal));
-        if ((rc = launch_sweep<T>(op, y, nullptr, nrhs, w, adj, order, block, s.active, st, rinv, shape, cf()))) return rc;
+        if ((rc = sweep(y, nullptr, s.active, st))) return rc;
         if (timed) H3D_CUDA_TRY(cudaEventRecordWithFlags(ev1, st, cudaEventRecordExternal));
         if ((rc = cg_ap_dot<T>(p, y, N, nrhs, s, st))) return rc;
         if ((rc = cg_update_xr<T>(x, r, p, y, N, nrhs, s, maxit, st))) return rc;
@@ -404,7 +444,7 @@ struct HostState {
     int init(int nrhs)
     {
         n = nrhs;
-        H3D_CUDA_TRY(cudaMallocHost(&h_ints, sizeof(int) * 3 * nrhs));
+        H3D_CUDA_TRY(cudaMallocHost(&h_ints, sizeof(int) * (3 * nrhs + 1)));
         H3D_CUDA_TRY(cudaMallocHost(&h_dbl, sizeof(double) * 4 * nrhs));
         active.resize(nrhs);
         iters.resize(nrhs);
@@ -415,6 +455,7 @@ struct HostState {
     template <typename T>
     int fetch(const CgRun<T> &cg, cudaStream_t st)
     {
+        if (cg.b8) H3D_CUDA_TRY(cudaMemcpyAsync(h_ints + 3 * n, cg.b8->err, sizeof(int), cudaMemcpyDeviceToHost, st));
         H3D_CUDA_TRY(cudaMemcpyAsync(h_ints, cg.s.active, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
         H3D_CUDA_TRY(cudaMemcpyAsync(h_ints + n, cg.s.iters, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
         H3D_CUDA_TRY(cudaMemcpyAsync(h_ints + 2 * n, cg.s.status, sizeof(int) * n, cudaMemcpyDeviceToHost, st));
@@ -425,6 +466,10 @@ struct HostState {
             iters[q] = h_ints[n + q];
             status[q] = h_ints[2 * n + q];
             ratio[q] = h_dbl[q];
+        }
+        if (cg.b8 && h_ints[3 * n]) {
+            set_error("a bounded wait of the batched BLOCK8 sweep expired (device status %d)", h_ints[3 * n]);
+            return H3D_ERR_TIMEOUT;
         }
         return H3D_OK;
     }
@@ -468,39 +513,105 @@ struct Timer {
 };
 
 // ---------------------------------------------------------------------------------------
-// Core solve on an internal stream.  b, u: complex128 interleaved device vectors.
-static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_im,
-                      const cplx<double> *b, cplx<double> *u, int nrhs, int mode,
-                      const h3d_solve_opts &o, h3d_solve_info *info, double *res_hist,
-                      int res_hist_len, cudaStream_t st)
+// One problem of a solve call: grid, FP64 wavenumber, complex128 b and u (device), columns.
+struct SolveProb {
+    h3d_grid g;
+    const double *wn_re, *wn_im;
+    const cplx<double> *b;
+    cplx<double> *u;
+    int nrhs, mode;
+};
+
+// Whether the problems run as one batched BLOCK8 solve: the order is BLOCK8 with the default
+// 12^3 blocks and the stored coefficients of every problem take at most half of the free
+// device memory.
+static bool use_batched_block8(const std::vector<SolveProb> &P, const h3d_solve_opts &o)
+{
+    if (o.order != H3D_ORDER_BLOCK8) return false;
+    const int32_t *bk = o.block;
+    if (!(bk[0] <= 0 || (bk[0] == 12 && bk[1] == 12 && bk[2] == 12))) return false;
+    size_t need = 0;
+    const size_t cs = o.precision == H3D_PREC_FP64 ? 16 : 8;
+    for (const SolveProb &p : P) {
+        const size_t nb = (size_t)((p.g.n[0] + 11) / 12) * ((p.g.n[1] + 11) / 12) * ((p.g.n[2] + 11) / 12) * 27 * 64;
+        need += nb * (27 * cs + cs / 2) + (size_t)p.g.n[0] * p.g.n[1] * p.g.n[2] * (cs / 2);
+    }
+    size_t fr = 0, tot = 0;
+    if (cudaMemGetInfo(&fr, &tot) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    return need <= fr / 2;
+}
+
+// Core solve of one or more problems on an internal stream.  With several problems the
+// order must be the batched BLOCK8 one (use_batched_block8).  infos: one entry per problem
+// (or null); the wall time is that of the whole call.
+static int solve_impl(const std::vector<SolveProb> &P, const h3d_solve_opts &o, h3d_solve_info *infos,
+                      double *res_hist, int res_hist_len, cudaStream_t st)
 {
     Timer timer;
     int rc;
-    Op<double> op64;
-    if ((rc = make_op_f64(g, wn_re, wn_im, &op64))) return rc;
-    const long long N = op64.N;
-    const bool adj = mode == H3D_ADJOINT;
+    const int np = (int)P.size();
+    const bool batched = use_batched_block8(P, o);
+    if (np > 1 && !batched) {
+        set_error("internal: several problems need the batched BLOCK8 solver");
+        return H3D_ERR_BAD_ARG;
+    }
+    std::vector<Op<double>> op64(np);
+    std::vector<long long> col0(np), Np(np);
+    std::vector<int> c0(np), Gr(np);
+    std::vector<size_t> poff(np);
+    long long L = 0, Nmax = 0;
+    int C = 0;
+    size_t ptot = 0;
+    for (int q = 0; q < np; ++q) {
+        if ((rc = make_op_f64(&P[q].g, P[q].wn_re, P[q].wn_im, &op64[q]))) return rc;
+        Np[q] = op64[q].N;
+        col0[q] = L;
+        c0[q] = C;
+        L += Np[q] * P[q].nrhs;
+        C += P[q].nrhs;
+        Nmax = std::max(Nmax, Np[q]);
+        Gr[q] = mvp_residual_parts(op64[q], P[q].nrhs);
+        poff[q] = ptot;
+        ptot += 2 * (size_t)Gr[q] * P[q].nrhs;
+    }
     const double zero_tol2 = 1e-24;  // (1e-12)^2, opAbstractMatrix.m:118
+    std::vector<int> colp(C);        // problem of each column
+    for (int q = 0; q < np; ++q)
+        for (int j = 0; j < P[q].nrhs; ++j) colp[c0[q] + j] = q;
 
-    // FP64 residual machinery: r64 = b - A u, per-RHS norms.
-    const int Gr = mvp_residual_parts(op64, nrhs);
+    // FP64 residual machinery: r64 = b - A u per problem (columns in the batch layout),
+    // per-column norms.
     DevBuf r64b, partb, normb;
-    if ((rc = r64b.alloc(sizeof(cplx<double>) * (size_t)N * nrhs, st))) return rc;
-    if ((rc = partb.alloc(sizeof(double) * 2 * (size_t)Gr * nrhs, st))) return rc;
-    if ((rc = normb.alloc(sizeof(double) * 2 * (size_t)nrhs, st))) return rc;
+    if ((rc = r64b.alloc(sizeof(cplx<double>) * (size_t)L, st))) return rc;
+    if ((rc = partb.alloc(sizeof(double) * ptot, st))) return rc;
+    if ((rc = normb.alloc(sizeof(double) * 2 * (size_t)C, st))) return rc;
     cplx<double> *r64 = r64b.as<cplx<double>>();
-    double *rr2 = normb.as<double>(), *bb2 = rr2 + nrhs;
-    H3D_CUDA_TRY(cudaMemsetAsync(u, 0, sizeof(cplx<double>) * (size_t)N * nrhs, st));
-    if ((rc = residual_f64(op64, b, u, r64, rr2, bb2, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
-    long long extra_launches = 2;
+    double *rr2 = normb.as<double>(), *bb2 = rr2 + C;
+    long long extra_launches = 0;
+    // r = b - A u for every problem; u_of(q) gives problem q's current solution columns
+    auto residual_all = [&](auto u_of, bool with_b) -> int {
+        for (int q = 0; q < np; ++q) {
+            int r = residual_f64(op64[q], P[q].b, u_of(q), r64 + col0[q], rr2 + c0[q], with_b ? bb2 + c0[q] : nullptr,
+                                 P[q].nrhs, P[q].mode == H3D_ADJOINT, partb.as<double>() + poff[q], Gr[q], st);
+            if (r) return r;
+        }
+        extra_launches += 2 * np;
+        return H3D_OK;
+    };
+    for (int q = 0; q < np; ++q)
+        H3D_CUDA_TRY(cudaMemsetAsync(P[q].u, 0, sizeof(cplx<double>) * (size_t)Np[q] * P[q].nrhs, st));
+    if ((rc = residual_all([&](int q) { return (const cplx<double> *)P[q].u; }, true))) return rc;
     double sw_sec = 0.0;
     int sw_n = 0, sw_variant = -1;
     long long cg_launches = 0;
 
-    std::vector<double> h_rr(nrhs), h_bb(nrhs);
+    std::vector<double> h_rr(C), h_bb(C);
     auto fetch_norms = [&]() -> int {
-        H3D_CUDA_TRY(cudaMemcpyAsync(h_rr.data(), rr2, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
-        H3D_CUDA_TRY(cudaMemcpyAsync(h_bb.data(), bb2, sizeof(double) * nrhs, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaMemcpyAsync(h_rr.data(), rr2, sizeof(double) * C, cudaMemcpyDeviceToHost, st));
+        H3D_CUDA_TRY(cudaMemcpyAsync(h_bb.data(), bb2, sizeof(double) * C, cudaMemcpyDeviceToHost, st));
         H3D_CUDA_TRY(cudaStreamSynchronize(st));
         return H3D_OK;
     };
@@ -508,64 +619,96 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
     const std::vector<double> bnorm2 = h_bb;
 
     HostState hs;
-    if ((rc = hs.init(nrhs))) return rc;
+    if ((rc = hs.init(C))) return rc;
     int hist_pos = 0;
-    int total_iters_max = 0, outer = 0;
-    std::vector<int> total_iters(nrhs, 0);
-    double last_prec = 0.0;
+    int outer = 0;
+    std::vector<int> total_iters(C, 0);
+    std::vector<double> last_prec(C, 0.0);
     bool nonfinite = false;
-    std::vector<int> done(nrhs, 0);
-    for (int q = 0; q < nrhs; ++q) done[q] = bnorm2[q] < zero_tol2;
+    std::vector<int> done(C, 0);
+    for (int c = 0; c < C; ++c) done[c] = bnorm2[c] < zero_tol2;
 
-    auto true_ok = [&](int q) { return h_bb[q] > 0 ? std::sqrt(h_rr[q] / bnorm2[q]) <= o.tol : true; };
-
-    if (o.precision == H3D_PREC_FP64) {
-        CgRun<double> cg;
-        cg.op = op64;
-        cg.N = N;
-        cg.nrhs = nrhs;
-        cg.adj = adj;
-        cg.w = o.w;
+    auto true_ok = [&](int c) { return h_bb[c] > 0 ? std::sqrt(h_rr[c] / bnorm2[c]) <= o.tol : true; };
+    // the batch's CGMN instance over all columns
+    auto configure = [&](auto &cg, auto &batch, const auto &ops) -> int {
+        using TT = std::decay_t<decltype(cg.w)>;
+        cg.N = batched ? Nmax : Np[0];
+        cg.nrhs = C;
+        cg.w = (TT)o.w;
         cg.order = o.order;
         std::memcpy(cg.block, o.block, sizeof cg.block);
         cg.maxit = o.maxit;
         cg.method = o.method;
         cg.verbose = o.verbose;
-        if ((rc = cg.alloc(st))) return rc;
-        std::vector<double> tolp(nrhs, o.tol);
-        H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, st));
-        if ((rc = cg.setup(b, bb2, zero_tol2, st))) return rc;
+        if (batched) {
+            for (int q = 0; q < np; ++q) batch.add(ops[q], P[q].mode == H3D_ADJOINT, col0[q], c0[q], P[q].nrhs);
+            batch.verbose = o.verbose;
+            int r = batch.setup(st);
+            if (r) return r;
+            cg.b8 = &batch;
+            cg.L = L;
+            cg.coloff.resize(C);
+            cg.collen.resize(C);
+            for (int c = 0; c < C; ++c) {
+                const int q = colp[c];
+                cg.coloff[c] = col0[q] + (long long)(c - c0[q]) * Np[q];
+                cg.collen[c] = Np[q];
+            }
+        } else {
+            cg.op = ops[0];
+            cg.adj = P[0].mode == H3D_ADJOINT;
+        }
+        return cg.alloc(st);
+    };
+
+    if (o.precision == H3D_PREC_FP64) {
+        CgRun<double> cg;
+        B8Batch<double> batch;
+        if ((rc = configure(cg, batch, op64))) return rc;
+        // the right-hand sides in the batch layout (one problem: b itself)
+        DevBuf bcat;
+        const cplx<double> *bb = P[0].b;
+        if (np > 1) {
+            if ((rc = bcat.alloc(sizeof(cplx<double>) * (size_t)L, st))) return rc;
+            for (int q = 0; q < np; ++q)
+                H3D_CUDA_TRY(cudaMemcpyAsync(bcat.as<cplx<double>>() + col0[q], P[q].b,
+                                             sizeof(cplx<double>) * (size_t)Np[q] * P[q].nrhs, cudaMemcpyDeviceToDevice, st));
+            bb = bcat.as<cplx<double>>();
+        }
+        std::vector<double> tolp(C, o.tol);
+        H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * C, cudaMemcpyHostToDevice, st));
+        if ((rc = cg.setup(bb, bb2, zero_tol2, st))) return rc;
         for (;;) {
             if ((rc = cg_drive(cg, hs, o, res_hist, res_hist_len, &hist_pos, st))) return rc;
             ++outer;
-            if ((rc = residual_f64(op64, b, cg.x, r64, rr2, nullptr, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
-            extra_launches += 2;
+            if ((rc = residual_all([&](int q) { return (const cplx<double> *)(cg.x + col0[q]); }, false))) return rc;
             if ((rc = fetch_norms())) return rc;
             if (o.stop_rule != H3D_STOP_TRUE_RESIDUAL) break;
             bool again = false;
-            for (int q = 0; q < nrhs; ++q) {
-                if (done[q] || hs.status[q] || hs.iters[q] >= o.maxit) continue;
-                const double tr = std::sqrt(h_rr[q] / bnorm2[q]);
+            for (int c = 0; c < C; ++c) {
+                if (done[c] || hs.status[c] || hs.iters[c] >= o.maxit) continue;
+                const double tr = std::sqrt(h_rr[c] / bnorm2[c]);
                 if (tr <= o.tol) continue;
                 // Not there yet on the true residual: tighten this column's preconditioned
                 // tolerance in proportion and continue the same Krylov sequence.
-                tolp[q] = std::max(hs.ratio[q] * (o.tol / tr) * 0.5, 1e-15);
+                tolp[c] = std::max(hs.ratio[c] * (o.tol / tr) * 0.5, 1e-15);
                 again = true;
             }
             if (!again || outer > o.max_outer) break;
-            std::vector<int> act(nrhs, 0);
-            for (int q = 0; q < nrhs; ++q)
-                act[q] = (!done[q] && !hs.status[q] && hs.iters[q] < o.maxit &&
-                          std::sqrt(h_rr[q] / bnorm2[q]) > o.tol);
-            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, st));
-            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.active, act.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, st));
+            std::vector<int> act(C, 0);
+            for (int c = 0; c < C; ++c)
+                act[c] = (!done[c] && !hs.status[c] && hs.iters[c] < o.maxit && std::sqrt(h_rr[c] / bnorm2[c]) > o.tol);
+            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * C, cudaMemcpyHostToDevice, st));
+            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.active, act.data(), sizeof(int) * C, cudaMemcpyHostToDevice, st));
             H3D_CUDA_TRY(cudaStreamSynchronize(st));
         }
-        H3D_CUDA_TRY(cudaMemcpyAsync(u, cg.x, sizeof(cplx<double>) * (size_t)N * nrhs, cudaMemcpyDeviceToDevice, st));
-        for (int q = 0; q < nrhs; ++q) {
-            total_iters[q] = hs.iters[q];
-            last_prec = std::max(last_prec, hs.ratio[q]);
-            nonfinite |= hs.status[q] != 0;
+        for (int q = 0; q < np; ++q)
+            H3D_CUDA_TRY(cudaMemcpyAsync(P[q].u, cg.x + col0[q], sizeof(cplx<double>) * (size_t)Np[q] * P[q].nrhs,
+                                         cudaMemcpyDeviceToDevice, st));
+        for (int c = 0; c < C; ++c) {
+            total_iters[c] = hs.iters[c];
+            last_prec[c] = hs.ratio[c];
+            nonfinite |= hs.status[c] != 0;
         }
         sw_sec = cg.sweep_seconds;
         sw_n = cg.sweep_samples;
@@ -573,56 +716,57 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         cg_launches = cg.launches;
     } else {
         // Mixed precision: complex64 CGMN on the scaled FP64 residual, FP64 update and residual.
+        long long wtot = 0;
+        for (int q = 0; q < np; ++q) wtot += Np[q] * (P[q].wn_im ? 2 : 1);
         DevBuf wn32b, rhs32b;
-        if ((rc = wn32b.alloc(sizeof(float) * (size_t)N * (wn_im ? 2 : 1), st))) return rc;
-        float *wn32 = wn32b.as<float>();
-        if ((rc = cast<double, float>(wn_re, wn32, N, st))) return rc;
-        if (wn_im && (rc = cast<double, float>(wn_im, wn32 + N, N, st))) return rc;
-        extra_launches += wn_im ? 2 : 1;
-        Op<float> op32;
-        if ((rc = make_op_f32(g, wn32, wn_im ? wn32 + N : nullptr, &op32))) return rc;
-        if ((rc = rhs32b.alloc(sizeof(cplx<float>) * (size_t)N * nrhs, st))) return rc;
+        if ((rc = wn32b.alloc(sizeof(float) * (size_t)wtot, st))) return rc;
+        std::vector<Op<float>> op32(np);
+        long long wo = 0;
+        for (int q = 0; q < np; ++q) {
+            float *w32 = wn32b.as<float>() + wo;
+            if ((rc = cast<double, float>(P[q].wn_re, w32, Np[q], st))) return rc;
+            if (P[q].wn_im && (rc = cast<double, float>(P[q].wn_im, w32 + Np[q], Np[q], st))) return rc;
+            extra_launches += P[q].wn_im ? 2 : 1;
+            if ((rc = make_op_f32(&P[q].g, w32, P[q].wn_im ? w32 + Np[q] : nullptr, &op32[q]))) return rc;
+            wo += Np[q] * (P[q].wn_im ? 2 : 1);
+        }
+        if ((rc = rhs32b.alloc(sizeof(cplx<float>) * (size_t)L, st))) return rc;
         cplx<float> *rhs32 = rhs32b.as<cplx<float>>();
         CgRun<float> cg;
-        cg.op = op32;
-        cg.N = N;
-        cg.nrhs = nrhs;
-        cg.adj = adj;
-        cg.w = (float)o.w;
-        cg.order = o.order;
-        std::memcpy(cg.block, o.block, sizeof cg.block);
-        cg.maxit = o.maxit;
-        cg.method = o.method;
-        cg.verbose = o.verbose;
-        if ((rc = cg.alloc(st))) return rc;
+        B8Batch<float> batch;
+        if ((rc = configure(cg, batch, op32))) return rc;
         DevBuf actb;
-        if ((rc = actb.alloc(sizeof(int) * nrhs, st))) return rc;
+        if ((rc = actb.alloc(sizeof(int) * C, st))) return rc;
         int *outer_active = actb.as<int>();
-        std::vector<double> tolp(nrhs, o.inner_tol);
-        H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * nrhs, cudaMemcpyHostToDevice, st));
+        std::vector<double> tolp(C, o.inner_tol);
+        H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.tolp, tolp.data(), sizeof(double) * C, cudaMemcpyHostToDevice, st));
         for (outer = 0; outer < o.max_outer; ++outer) {
-            std::vector<int> act(nrhs, 0);
+            std::vector<int> act(C, 0);
             bool any = false;
-            for (int q = 0; q < nrhs; ++q) {
-                act[q] = !done[q] && !true_ok(q) && total_iters[q] < o.maxit;
-                any |= act[q] != 0;
+            for (int c = 0; c < C; ++c) {
+                act[c] = !done[c] && !true_ok(c) && total_iters[c] < o.maxit;
+                any |= act[c] != 0;
             }
             if (!any) break;
-            H3D_CUDA_TRY(cudaMemcpyAsync(outer_active, act.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, st));
-            if ((rc = scale_to_c64(r64, rhs32, N, nrhs, rr2, outer_active, st))) return rc;
+            H3D_CUDA_TRY(cudaMemcpyAsync(outer_active, act.data(), sizeof(int) * C, cudaMemcpyHostToDevice, st));
+            for (int q = 0; q < np; ++q)
+                if ((rc = scale_to_c64(r64 + col0[q], rhs32 + col0[q], Np[q], P[q].nrhs, rr2 + c0[q], outer_active + c0[q], st)))
+                    return rc;
             if ((rc = cg.setup(rhs32, nullptr, 0.0, st))) return rc;
             // only the columns still above tolerance iterate
-            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.active, act.data(), sizeof(int) * nrhs, cudaMemcpyHostToDevice, st));
+            H3D_CUDA_TRY(cudaMemcpyAsync(cg.s.active, act.data(), sizeof(int) * C, cudaMemcpyHostToDevice, st));
             if ((rc = cg_drive(cg, hs, o, res_hist, res_hist_len, &hist_pos, st))) return rc;
-            if ((rc = add_scaled_c64(u, cg.x, N, nrhs, rr2, outer_active, st))) return rc;
-            for (int q = 0; q < nrhs; ++q) {
-                if (!act[q]) continue;
-                total_iters[q] += hs.iters[q];
-                last_prec = hs.ratio[q];
-                nonfinite |= hs.status[q] != 0;
+            for (int q = 0; q < np; ++q)
+                if ((rc = add_scaled_c64(P[q].u, cg.x + col0[q], Np[q], P[q].nrhs, rr2 + c0[q], outer_active + c0[q], st)))
+                    return rc;
+            for (int c = 0; c < C; ++c) {
+                if (!act[c]) continue;
+                total_iters[c] += hs.iters[c];
+                last_prec[c] = hs.ratio[c];
+                nonfinite |= hs.status[c] != 0;
             }
-            if ((rc = residual_f64(op64, b, u, r64, rr2, nullptr, nrhs, adj, partb.as<double>(), Gr, st))) return rc;
-            extra_launches += 4;  // scale, add, residual (2)
+            if ((rc = residual_all([&](int q) { return (const cplx<double> *)P[q].u; }, false))) return rc;
+            extra_launches += 2 * np;  // scale, add
             if ((rc = fetch_norms())) return rc;
             if (nonfinite) break;
         }
@@ -632,58 +776,102 @@ static int solve_impl(const h3d_grid *g, const double *wn_re, const double *wn_i
         cg_launches = cg.launches;
     }
     bool all_ok = !nonfinite;
-    double worst = 0.0;
-    for (int q = 0; q < nrhs; ++q) {
-        total_iters_max = std::max(total_iters_max, total_iters[q]);
-        if (done[q]) {
-            H3D_CUDA_TRY(cudaMemsetAsync(u + (size_t)q * N, 0, sizeof(cplx<double>) * (size_t)N, st));
+    std::vector<double> worst(np, 0.0), prec(np, 0.0);
+    std::vector<int> iters_max(np, 0);
+    std::vector<bool> ok(np, !nonfinite);
+    for (int c = 0; c < C; ++c) {
+        const int q = colp[c];
+        iters_max[q] = std::max(iters_max[q], total_iters[c]);
+        prec[q] = std::max(prec[q], last_prec[c]);
+        if (done[c]) {
+            H3D_CUDA_TRY(cudaMemsetAsync(P[q].u + (size_t)(c - c0[q]) * Np[q], 0, sizeof(cplx<double>) * (size_t)Np[q], st));
             continue;
         }
-        const double tr = std::sqrt(h_rr[q] / bnorm2[q]);
-        worst = std::max(worst, tr);
-        if (o.stop_rule == H3D_STOP_TRUE_RESIDUAL ? !(tr <= o.tol) : false) all_ok = false;
+        const double tr = std::sqrt(h_rr[c] / bnorm2[c]);
+        worst[q] = std::max(worst[q], tr);
+        if (o.stop_rule == H3D_STOP_TRUE_RESIDUAL ? !(tr <= o.tol) : false) {
+            all_ok = false;
+            ok[q] = false;
+        }
     }
     H3D_CUDA_TRY(cudaStreamSynchronize(st));
-    if (info) {
-        info->iters = total_iters_max;
-        info->outer = outer;
-        info->converged = all_ok ? 1 : 0;
-        info->nrhs = nrhs;
-        info->rel_res_true = worst;
-        info->rel_res_prec = last_prec;
-        info->seconds = timer.seconds();
-        info->sweep_seconds = sw_sec;
-        info->sweep_samples = sw_n;
-        info->sweep_variant = sw_variant;
-        info->kernel_launches = extra_launches + cg_launches;
+    const double secs = timer.seconds();
+    for (int q = 0; infos && q < np; ++q) {
+        h3d_solve_info &in = infos[q];
+        in.iters = iters_max[q];
+        in.outer = outer;
+        in.converged = ok[q] ? 1 : 0;
+        in.nrhs = P[q].nrhs;
+        in.rel_res_true = worst[q];
+        in.rel_res_prec = prec[q];
+        in.seconds = secs;
+        in.sweep_seconds = sw_sec;
+        in.sweep_samples = sw_n;
+        in.sweep_variant = sw_variant;
+        in.kernel_launches = q == 0 ? extra_launches + cg_launches : 0;
     }
     if (nonfinite) {
         set_error("non-finite value in the CGMN iteration");
         return H3D_ERR_NONFINITE;
     }
     if (!all_ok) {
-        set_error("not converged: max true relative residual %.3e after %d iterations", worst, total_iters_max);
+        double w = 0.0;
+        int it = 0;
+        for (int q = 0; q < np; ++q) {
+            w = std::max(w, worst[q]);
+            it = std::max(it, iters_max[q]);
+        }
+        set_error("not converged: max true relative residual %.3e after %d iterations", w, it);
         return H3D_ERR_NOT_CONVERGED;
     }
     return H3D_OK;
 }
 
-// Run f on an internal non-blocking stream ordered after the caller's stream.
+// The calling thread's internal non-blocking stream and event on the current device, created
+// on first use and kept for the thread's lifetime (solves of the FWI layer come in long runs).
+struct InternalStream {
+    int dev = -1;
+    cudaStream_t st = nullptr;
+    cudaEvent_t ev = nullptr;
+    ~InternalStream() { release(); }
+    void release()
+    {
+        if (ev) cudaEventDestroy(ev);
+        if (st) cudaStreamDestroy(st);
+        ev = nullptr;
+        st = nullptr;
+    }
+    int get(cudaStream_t *s, cudaEvent_t *e)
+    {
+        int d = 0;
+        H3D_CUDA_TRY(cudaGetDevice(&d));
+        if (d != dev || !st) {
+            release();
+            H3D_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+            H3D_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+            dev = d;
+        }
+        *s = st;
+        *e = ev;
+        return H3D_OK;
+    }
+};
+static thread_local InternalStream g_internal;
+
+// Run f on the internal stream, ordered after the caller's stream and before its later work.
 template <typename F>
 static int on_internal_stream(cudaStream_t user, F f)
 {
     cudaStream_t st = nullptr;
     cudaEvent_t ev = nullptr;
-    H3D_CUDA_TRY(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
-    H3D_CUDA_TRY(cudaEventCreateWithFlags(&ev, cudaEventDisableTiming));
+    int rc = g_internal.get(&st, &ev);
+    if (rc) return rc;
     H3D_CUDA_TRY(cudaEventRecord(ev, user));
     H3D_CUDA_TRY(cudaStreamWaitEvent(st, ev, 0));
-    int rc = f(st);
+    rc = f(st);
     cudaError_t e1 = cudaEventRecord(ev, st);
     cudaError_t e2 = cudaStreamWaitEvent(user, ev, 0);
     cudaError_t e3 = cudaStreamSynchronize(st);
-    cudaEventDestroy(ev);
-    cudaStreamDestroy(st);
     if (rc) return rc;
     if (e1 != cudaSuccess) return cuda_fail(e1, "cudaEventRecord");
     if (e2 != cudaSuccess) return cuda_fail(e2, "cudaStreamWaitEvent");
@@ -747,10 +935,9 @@ int h3d_solve(const h3d_grid *g, const double *wn_re, const double *wn_im, const
     h3d_solve_opts o;
     h3d_default_opts(&o);
     if (opts) o = *opts;
-    return on_internal_stream((cudaStream_t)stream, [&](cudaStream_t st) {
-        return solve_impl(g, wn_re, wn_im, (const cplx<double> *)b, (cplx<double> *)u, nrhs, mode, o,
-                          info, res_hist, res_hist_len, st);
-    });
+    std::vector<SolveProb> P{{*g, wn_re, wn_im, (const cplx<double> *)b, (cplx<double> *)u, nrhs, mode}};
+    return on_internal_stream((cudaStream_t)stream,
+                              [&](cudaStream_t st) { return solve_impl(P, o, info, res_hist, res_hist_len, st); });
 }
 
 int h3d_solve_batch(const h3d_problem *probs, int nprob, const h3d_solve_opts *opts,
@@ -760,15 +947,34 @@ int h3d_solve_batch(const h3d_problem *probs, int nprob, const h3d_solve_opts *o
         set_error("h3d_solve_batch: bad argument");
         return H3D_ERR_BAD_ARG;
     }
-    int worst = H3D_OK;
+    int rc;
+    if ((rc = check_opts(opts))) return rc;
+    h3d_solve_opts o;
+    h3d_default_opts(&o);
+    if (opts) o = *opts;
+    std::vector<SolveProb> P;
     for (int q = 0; q < nprob; ++q) {
         const h3d_problem &p = probs[q];
-        int rc = h3d_solve(&p.grid, p.wn_re, p.wn_im, p.b, p.u, p.nrhs, p.mode, opts,
-                           infos ? &infos[q] : nullptr, nullptr, 0, stream);
-        if (rc && rc != H3D_ERR_NOT_CONVERGED) return rc;
-        if (rc) worst = rc;
+        if ((rc = check_grid(&p.grid))) return rc;
+        if (!p.wn_re || !p.b || !p.u || p.nrhs < 1 || (p.mode != H3D_FORWARD && p.mode != H3D_ADJOINT)) {
+            set_error("h3d_solve_batch: bad argument in problem %d", q);
+            return H3D_ERR_BAD_ARG;
+        }
+        P.push_back({p.grid, p.wn_re, p.wn_im, (const cplx<double> *)p.b, (cplx<double> *)p.u, p.nrhs, p.mode});
     }
-    return worst;
+    return on_internal_stream((cudaStream_t)stream, [&](cudaStream_t st) -> int {
+        // all problems in one batched BLOCK8 solve when the order and memory allow it,
+        // otherwise one solve after another
+        if (nprob > 1 && use_batched_block8(P, o)) return solve_impl(P, o, infos, nullptr, 0, st);
+        int worst = H3D_OK;
+        for (int q = 0; q < nprob; ++q) {
+            std::vector<SolveProb> one{P[q]};
+            int r = solve_impl(one, o, infos ? &infos[q] : nullptr, nullptr, 0, st);
+            if (r && r != H3D_ERR_NOT_CONVERGED) return r;
+            if (r) worst = r;
+        }
+        return worst;
+    });
 }
 
 int h3d_solve_host(const h3d_grid *g, const double *wn_re, const double *wn_im,

@@ -80,6 +80,7 @@ _SIGS = {
     "h3d_residual": (C.c_int, [C.POINTER(Grid), vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int, vp]),
     "h3d_residual_noalloc": (C.c_int, [C.POINTER(Grid), vp, vp, vp, vp, vp, vp, vp, C.c_int, C.c_int,
                                        vp]),
+    "h3d_check_wait_timeout": (C.c_int, [C.c_double]),
     "h3d_mex_mvp": (C.c_int, [dp, dp, dp, dp, C.c_size_t, dp, dp, dp, C.c_size_t, dp, dp, C.c_int,
                               C.c_int]),
     "h3d_mex_kacz_sweep": (C.c_int, [dp, dp, dp, dp, C.c_size_t, dp, C.c_double, dp, dp,

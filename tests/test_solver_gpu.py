@@ -164,3 +164,58 @@ def test_point_source_matches_analytic_greens_function(cuda):
     r[c, c, c] = 0.0                      # the wavefield is not expected to be accurate at the source
     s = slice(npml, npml + nphys)
     assert np.linalg.norm(r[s, s, s]) / np.linalg.norm(U[s, s, s]) < 0.01
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_batched_block8_uneven_problems(cuda, precision):
+    """Three problems of different grids, PML widths, modes, wavenumber kinds and column
+    counts (9 columns: a full group of eight and a partly filled one) in one batched BLOCK8
+    solve: every column reaches the true residual 1e-6 (checked by the oracle's matvec) and
+    agrees with the oracle's tight solution; a zero column returns zero."""
+    import torch
+    from h3d import solver
+
+    specs = [((30, 26, 28), 4, 9, 1, False), ((21, 25, 19), 3, 1, 2, False), ((27, 27, 27), 5, 3, 1, True)]
+    probs, refs = [], []
+    for q, (n, npml, P, mode, wnc) in enumerate(specs):
+        grid, g, wn, b = _problem(n=n, npml=npml, seed=50 + q)
+        if wnc:
+            wn = wn * (1.0 + 0.02j)
+        rng = np.random.default_rng(60 + q)
+        B = np.stack([b] + [rng.standard_normal(b.size) + 1j * rng.standard_normal(b.size) for _ in range(P - 1)])
+        if P >= 3:
+            B[1] = 0.0
+        probs.append(solver.Problem(grid, _t(wn, cuda), _t(B, cuda), mode=mode))
+        refs.append((g, wn, B, mode))
+    us, infos = solver.solve_batch(probs, tol=1e-6, precision=precision)
+    for u, info, (g, wn, B, mode) in zip(us, infos, refs):
+        assert info["converged"] == 1
+        U = u.cpu().numpy()
+        for s in range(B.shape[0]):
+            if not np.any(B[s]):
+                assert np.all(U[s] == 0)
+                continue
+            assert slim_ref.true_residual(g, wn, B[s], U[s], mode=mode) <= 1e-6
+        xref = slim_ref.cgmn_solve(g, wn, B[0], tol=1e-11, maxit=8000, mode=mode, order=O.ORDER_COLOUR27)
+        assert np.linalg.norm(U[0] - xref) / np.linalg.norm(xref) <= 1e-4
+
+
+def test_bounded_wait_expires_with_a_status(cuda):
+    """The BLOCK8 kernel's bounded mbarrier waits: a coefficient copy announced but never
+    issued makes every wait of the first colour step give up after 2 ms; the call returns
+    H3D_ERR_TIMEOUT and the context stays usable (a sweep right after matches the oracle)."""
+    import torch
+    from h3d import _lib as L
+    from h3d import ops
+
+    lib = L.load()
+    assert lib.h3d_check_wait_timeout(2.0) == L.ERR_TIMEOUT
+    assert b"expired" in lib.h3d_last_error()
+    torch.cuda.synchronize()
+    n, npml = (26, 25, 27), 4
+    grid, g, wn, b = _problem(n=n, npml=npml, seed=70)
+    rng = np.random.default_rng(71)
+    X = rng.standard_normal(b.size) + 1j * rng.standard_normal(b.size)
+    ref = O.sweep(g, wn, 1.5, X, b, order=O.ORDER_BLOCK8, blk=(12, 12, 12), nthreads=2)
+    y = ops.kacz_sweep(grid, _t(wn, cuda), 1.5, _t(X, cuda), _t(b, cuda), 1, order=3)
+    assert np.linalg.norm(y.cpu().numpy() - ref) / np.linalg.norm(ref) <= 1e-12
