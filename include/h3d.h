@@ -139,6 +139,9 @@ typedef struct h3d_solve_info {
     int32_t sweep_variant;  /* kernel configuration the tuner chose: COLOUR27 tile shape 0-3 or
                                4 = stored row coefficients; BLOCK / BLOCK8 configuration */
     int64_t kernel_launches;/* device kernels this call executed (graph replays included) */
+    double sweep_bytes;     /* algorithmic bytes of the timed double sweeps (sweep_seconds):
+                               per sweep, x read and written once per active right-hand side
+                               and the wavenumber read once per problem with an active one */
 } h3d_solve_info;
 
 /* One problem of a batched solve: its own grid, wavenumber and right-hand sides. */
@@ -234,7 +237,9 @@ int h3d_solve(const h3d_grid *g, const double *wn_re, const double *wn_im, const
               void *u, int nrhs, int mode, const h3d_solve_opts *opts, h3d_solve_info *info,
               double *res_hist, int res_hist_len, void *stream);
 
-/* Solve every problem of the table; infos (host, nprob entries) may be NULL.  With the BLOCK8
+/* Solve every problem of the table; infos (host, nprob entries) may be NULL (a batched solve
+ * reports its sweep timing, sweep bytes and kernel launches in the first entry and zero in the
+ * others).  With the BLOCK8
  * order (12^3 blocks) and room for every problem's stored coefficients in device memory, all
  * problems run as one batched solve: their columns iterate together (each with its own
  * convergence mask), and every sweep launch covers all problems; problems may differ in grid,

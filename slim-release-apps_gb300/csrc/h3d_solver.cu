@@ -93,6 +93,7 @@ struct CgRun {
     int nrhs = 0;      // columns
     B8Batch<T> *b8 = nullptr;           // batched BLOCK8 sweeps (null: sweeps of op)
     std::vector<long long> coloff, collen;  // batched: column map (host copy)
+    std::vector<int> colprob;               // batched: problem of each column
     bool b8_tuned = false;
     bool adj = false;
     T w = T(1.5);
@@ -116,6 +117,8 @@ struct CgRun {
     bool timed_pending = false;
     double sweep_seconds = 0.0;
     int sweep_samples = 0;
+    double pending_bytes = 0.0;  // algorithmic bytes of the timed sweep of the running block
+    double sweep_bytes = 0.0;
     long long launches = 0;        // kernels executed by this instance
     long long block_launches = 0;  // kernels in one replayed block
 
@@ -135,6 +138,7 @@ struct CgRun {
         float ms = 0.f;
         if (cudaEventElapsedTime(&ms, ev0, ev1) == cudaSuccess) {
             sweep_seconds += 1e-3 * ms;
+            sweep_bytes += pending_bytes;
             ++sweep_samples;
         }
         timed_pending = false;
@@ -220,6 +224,32 @@ struct CgRun {
     {
         if (b8) return b8->dsweep(v, b, w, act, st);
         return launch_sweep<T>(op, v, b, nrhs, w, adj, order, block, act, st, rinv, shape, cf());
+    }
+
+    // Algorithmic bytes of one double sweep over the columns flagged in act (host flags):
+    // 2 (read + write) complex values of x per active column and point, plus one read of
+    // the wavenumber per point of every problem with an active column, in each direction.
+    double dsweep_bytes(const std::vector<int> &act) const
+    {
+        const double sc = sizeof(cplx<T>);
+        if (!b8) {
+            long long na = 0;
+            for (int c = 0; c < nrhs; ++c) na += act[c] != 0;
+            const double sw = sizeof(T) * (op.wni ? 2 : 1);
+            return na ? 2.0 * (double)N * (2.0 * sc * na + sw) : 0.0;
+        }
+        double bytes = 0.0;
+        std::vector<char> seen(b8->items.size(), 0);
+        for (int c = 0; c < nrhs; ++c) {
+            if (!act[c]) continue;
+            bytes += 2.0 * (double)collen[c] * 2.0 * sc;
+            const int q = colprob[c];
+            if (!seen[q]) {
+                seen[q] = 1;
+                bytes += 2.0 * (double)collen[c] * sizeof(T) * (b8->items[q].op.wni ? 2 : 1);
+            }
+        }
+        return bytes;
     }
 
     int sweep_launches() const
@@ -500,6 +530,7 @@ static int cg_drive(CgRun<T> &cg, HostState &hs, const h3d_solve_opts &o, double
             fprintf(stderr, "[h3d] cgmn(%s) it %d max-ratio %.3e\n", sizeof(T) == 8 ? "c128" : "c64", it, mx);
         }
         if (!any) return H3D_OK;
+        cg.pending_bytes = cg.dsweep_bytes(hs.active);
         if ((rc = cg.run_block(block_iters, o.use_graphs != 0, st))) return rc;
     }
 }
@@ -604,7 +635,7 @@ static int solve_impl(const std::vector<SolveProb> &P, const h3d_solve_opts &o, 
     for (int q = 0; q < np; ++q)
         H3D_CUDA_TRY(cudaMemsetAsync(P[q].u, 0, sizeof(cplx<double>) * (size_t)Np[q] * P[q].nrhs, st));
     if ((rc = residual_all([&](int q) { return (const cplx<double> *)P[q].u; }, true))) return rc;
-    double sw_sec = 0.0;
+    double sw_sec = 0.0, sw_bytes = 0.0;
     int sw_n = 0, sw_variant = -1;
     long long cg_launches = 0;
 
@@ -649,6 +680,7 @@ static int solve_impl(const std::vector<SolveProb> &P, const h3d_solve_opts &o, 
             cg.L = L;
             cg.coloff.resize(C);
             cg.collen.resize(C);
+            cg.colprob = colp;
             for (int c = 0; c < C; ++c) {
                 const int q = colp[c];
                 cg.coloff[c] = col0[q] + (long long)(c - c0[q]) * Np[q];
@@ -711,6 +743,7 @@ static int solve_impl(const std::vector<SolveProb> &P, const h3d_solve_opts &o, 
             nonfinite |= hs.status[c] != 0;
         }
         sw_sec = cg.sweep_seconds;
+        sw_bytes = cg.sweep_bytes;
         sw_n = cg.sweep_samples;
         sw_variant = cg.shape;
         cg_launches = cg.launches;
@@ -771,6 +804,7 @@ static int solve_impl(const std::vector<SolveProb> &P, const h3d_solve_opts &o, 
             if (nonfinite) break;
         }
         sw_sec = cg.sweep_seconds;
+        sw_bytes = cg.sweep_bytes;
         sw_n = cg.sweep_samples;
         sw_variant = cg.shape;
         cg_launches = cg.launches;
@@ -805,8 +839,11 @@ static int solve_impl(const std::vector<SolveProb> &P, const h3d_solve_opts &o, 
         in.rel_res_true = worst[q];
         in.rel_res_prec = prec[q];
         in.seconds = secs;
-        in.sweep_seconds = sw_sec;
-        in.sweep_samples = sw_n;
+        // the batch's sweep timing and launch count go to the first problem's entry only, so
+        // that sums over the entries count them once
+        in.sweep_seconds = q == 0 ? sw_sec : 0.0;
+        in.sweep_bytes = q == 0 ? sw_bytes : 0.0;
+        in.sweep_samples = q == 0 ? sw_n : 0;
         in.sweep_variant = sw_variant;
         in.kernel_launches = q == 0 ? extra_launches + cg_launches : 0;
     }

@@ -43,7 +43,7 @@ class SolveInfo(C.Structure):
         ("iters", C.c_int32), ("outer", C.c_int32), ("converged", C.c_int32), ("nrhs", C.c_int32),
         ("rel_res_true", C.c_double), ("rel_res_prec", C.c_double), ("seconds", C.c_double),
         ("sweep_seconds", C.c_double), ("sweep_samples", C.c_int32), ("sweep_variant", C.c_int32),
-        ("kernel_launches", C.c_int64),
+        ("kernel_launches", C.c_int64), ("sweep_bytes", C.c_double),
     ]
 
     def as_dict(self):

@@ -11,10 +11,12 @@ Mirrors ``[f,g] = PDEfunc(PDEopts.OBJ, v, Q, [], Dobs, model, params)`` and
                     V   = H' \\ (-Pr' dphi)                               (PDEfunc.m:393)
                     g  += crop( Re(conj(U) .* (dH' V)) )                  (PDEfunc.m:394, discrete_helmholtz.m:288)
 
-The sources of one frequency are solved together as one batch of right-hand sides; the
-gradient accumulation over the batch is one fused kernel (h3d_grad_accum).  Forward
-wavefields are kept for the gradient while they fit an HBM budget and recomputed
-otherwise.  Everything runs through libh3d.so's C ABI.
+The sources of one frequency are right-hand sides of one problem, and (CGMN solver, wavefields
+within the HBM budget) the problems of all frequencies are solved as one batch
+(h3d_solve_batch: every sweep launch covers all frequencies); the gradient accumulation over
+a source batch is one fused kernel (h3d_grad_accum).  Forward wavefields are kept for the
+gradient while they fit an HBM budget and recomputed otherwise.  Everything runs through
+libh3d.so's C ABI.
 """
 from __future__ import annotations
 
@@ -224,6 +226,17 @@ class FWIProblem:
         v = v_phys.detach().to(torch.float64).cpu().numpy().reshape(self.geom.n)
         return MG.build_levels(v, self.geom.d, npml.pop(), freq, self.geom.unit, device=self.dev)
 
+    def _solve_many(self, jobs):
+        """Solve every (wn, b, mode) of ``jobs``: one batched call over all of them (the CGMN
+        solver: frequencies and source batches iterate together, one sweep launch per block
+        parity covering every problem); returns the solutions in order."""
+        if self.cfg.solver != "cgmn" or len(jobs) == 1:
+            return [self._solve(wn, b, mode) for wn, b, mode in jobs]
+        probs = [S.Problem(self.g, wn, b, mode) for wn, b, mode in jobs]
+        us, infos = S.solve_batch(probs, opts=self._opts())
+        self.last_infos.extend(infos)
+        return us
+
     def _solve(self, wn, b, mode, ml=None):
         if ml is None:
             u, info = S.solve(self.g, wn, b, mode=mode, opts=self._opts())
@@ -264,40 +277,61 @@ class FWIProblem:
     def wavefield_bytes(self) -> float:
         return 16.0 * self.N * self.nsrc * len(self.geom.freqs)
 
+    def _units(self):
+        """(frequency index, source list) of every batch, in the reference's column order."""
+        return [(k, srcs) for k in range(len(self.geom.freqs)) for srcs in self._batches()]
+
     def misfit_forward(self, v_phys: torch.Tensor, Dobs: torch.Tensor, keep: bool):
-        """f and the data residuals; keeps the forward wavefields when ``keep``."""
+        """f and the data residuals; keeps the forward wavefields when ``keep``.  With the CGMN
+        solver and the wavefields kept, every frequency's forward solves run as one batch."""
         f = 0.0
         resid, fields = [], []
+        units = self._units()
+        if keep and self.cfg.solver == "cgmn":
+            wns = [self._wavenumbers(v_phys, float(fr))[0] for fr in self.geom.freqs]
+            Us = self._solve_many([(wns[k], self._sources(k, srcs), 1) for k, srcs in units])
+        else:
+            Us = None
         col = 0
-        for k, fr in enumerate(self.geom.freqs):
-            wn, _ = self._wavenumbers(v_phys, float(fr))
-            ml = self._levels(v_phys, float(fr))
-            for srcs in self._batches():
-                U = self._solve(wn, self._sources(k, srcs), 1, ml)
-                dpred = self._sample(U)
-                dobs = Dobs[:, col:col + len(srcs)].T.to(torch.complex128)
-                r = dpred - dobs                                     # LS_misfit.m:23
-                f += 0.5 * float(torch.sum(r.real ** 2 + r.imag ** 2))   # LS_misfit.m:24
-                resid.append(r)
-                fields.append(U if keep else None)
-                col += len(srcs)
+        for q, (k, srcs) in enumerate(units):
+            if Us is not None:
+                U = Us[q]
+            else:
+                fr = float(self.geom.freqs[k])
+                wn, _ = self._wavenumbers(v_phys, fr)
+                U = self._solve(wn, self._sources(k, srcs), 1, self._levels(v_phys, fr))
+            dpred = self._sample(U)
+            dobs = Dobs[:, col:col + len(srcs)].T.to(torch.complex128)
+            r = dpred - dobs                                     # LS_misfit.m:23
+            f += 0.5 * float(torch.sum(r.real ** 2 + r.imag ** 2))   # LS_misfit.m:24
+            resid.append(r)
+            fields.append(U if keep else None)
+            col += len(srcs)
         return f, resid, fields
 
     def gradient(self, v_phys: torch.Tensor, resid, fields):
-        """g (physical grid, x-fastest flat) from the residuals; recomputes U where not kept."""
+        """g (physical grid, x-fastest flat) from the residuals; recomputes U where not kept.
+        With the CGMN solver and the forward wavefields kept, every frequency's adjoint solves
+        run as one batch."""
         n = self.geom.n
         g = torch.zeros(int(np.prod(n)), dtype=torch.float64, device=self.dev)
-        q = 0
-        for k, fr in enumerate(self.geom.freqs):
-            wn, dwn = self._wavenumbers(v_phys, float(fr))
-            ml = self._levels(v_phys, float(fr))
-            for srcs in self._batches():
-                U = fields[q]
-                if U is None:
-                    U = self._solve(wn, self._sources(k, srcs), 1, ml)   # recompute above the budget
-                V = self._solve(wn, self._spread(resid[q], -1.0), 2, ml)   # H' \ (-Pr' dphi)
-                self._grad_accum(dwn, U, V, g)
-                q += 1
+        units = self._units()
+        if all(U is not None for U in fields) and self.cfg.solver == "cgmn":
+            wd = [self._wavenumbers(v_phys, float(fr)) for fr in self.geom.freqs]
+            Vs = self._solve_many([(wd[k][0], self._spread(resid[q], -1.0), 2)       # H' \ (-Pr' dphi)
+                                   for q, (k, _) in enumerate(units)])
+            for q, (k, _) in enumerate(units):
+                self._grad_accum(wd[k][1], fields[q], Vs[q], g)
+            return g
+        for q, (k, srcs) in enumerate(units):
+            fr = float(self.geom.freqs[k])
+            wn, dwn = self._wavenumbers(v_phys, fr)
+            ml = self._levels(v_phys, fr)
+            U = fields[q]
+            if U is None:
+                U = self._solve(wn, self._sources(k, srcs), 1, ml)   # recompute above the budget
+            V = self._solve(wn, self._spread(resid[q], -1.0), 2, ml)   # H' \ (-Pr' dphi)
+            self._grad_accum(dwn, U, V, g)
         return g
 
     def objective_pairs(self, v_phys: torch.Tensor, Dobs: torch.Tensor, k: int, srcs):

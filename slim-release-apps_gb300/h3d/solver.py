@@ -110,8 +110,9 @@ class Problem:
     mode: int = 1
 
 
-def solve_batch(problems, opts: L.SolveOpts | None = None, **kw):
-    """Solve a list of Problems of uneven size; returns (list of u, list of info dicts)."""
+def solve_batch(problems, opts: L.SolveOpts | None = None, raise_not_converged: bool = True, **kw):
+    """Solve a list of Problems of uneven size; returns (list of u, list of info dicts).  With the
+    BLOCK8 order all problems iterate together (h3d_solve_batch)."""
     o = opts if opts is not None else make_opts(**kw)
     arr = (L.Problem * len(problems))()
     keep, outs = [], []
@@ -134,5 +135,6 @@ def solve_batch(problems, opts: L.SolveOpts | None = None, **kw):
     infos = (L.SolveInfo * len(problems))()
     rc = L.load().h3d_solve_batch(arr, len(problems), C.byref(o), infos,
                                   C.c_void_p(torch.cuda.current_stream().cuda_stream))
-    L.check(rc, "h3d_solve_batch")
+    if not (rc == L.ERR_NOT_CONVERGED and not raise_not_converged):
+        L.check(rc, "h3d_solve_batch")
     return outs, [i.as_dict() for i in infos]

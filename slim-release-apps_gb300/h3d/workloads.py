@@ -11,6 +11,7 @@ Config 1 (one source, the headline) is bench.py's workload.
 from __future__ import annotations
 
 import argparse
+import ctypes as C
 import json
 import time
 
@@ -19,20 +20,33 @@ import torch
 
 from . import _lib as L
 from . import fwi, models, solver
+from . import solver as S
 
 
 def _events():
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
-def config2(order="block8", precision="mixed", freqs=None, nsrc=None, tol=1e-6, inner_tol=1e-4):
-    """64 surface sources x {3,4,5,6} Hz on the config-1 model: one problem per frequency,
-    the sources of a frequency as right-hand sides of one batched solve."""
+def _summary(infos, seconds):
+    """Throughput figures of one batched solve: the live sweep roofline (algorithmic bytes of the
+    timed double sweeps over their device time) and the iteration counts."""
+    sb = sum(i["sweep_bytes"] for i in infos)          # a batch reports its timing in the first entry
+    ss = sum(i["sweep_seconds"] for i in infos)
+    return {"seconds": seconds, "iters": [i["iters"] for i in infos],
+            "rel_res_true_max": max(i["rel_res_true"] for i in infos),
+            "sweep_gbs": (sb / ss / 1e9) if ss > 0 else None,
+            "sweep_samples": sum(i["sweep_samples"] for i in infos),
+            "kernel_launches": int(sum(i["kernel_launches"] for i in infos))}
+
+
+def config2_problems(freqs=None, nsrc=None, src0=0):
+    """64 surface sources x {3,4,5,6} Hz on the config-1 model: one problem per frequency, its
+    sources (Ricker-weighted unit impulses) as right-hand sides."""
     m = models.config2()
     dev = torch.device("cuda:0")
     fr = m.meta["freqs"] if freqs is None else np.asarray(freqs)
     wts = models.ricker_weight(fr, 8.0)
-    srcs = m.sources if nsrc is None else m.sources[:nsrc]
+    srcs = m.sources[src0:] if nsrc is None else m.sources[src0:src0 + nsrc]
     nx, ny, _ = m.n_total
     probs = []
     for f, wgt in zip(fr, wts):
@@ -41,20 +55,40 @@ def config2(order="block8", precision="mixed", freqs=None, nsrc=None, tol=1e-6, 
         for s, (i, j, k) in enumerate(srcs):
             b[s, int(i) + nx * int(j) + nx * ny * int(k)] = complex(wgt)
         probs.append(solver.Problem((m.n_total, m.h, m.npml6), wn, b, 1))
-    opts = solver.make_opts(tol=tol, precision=precision, order=order, inner_tol=inner_tol)
-    solver.solve_batch(probs[:1], opts=opts)            # warm-up (autotuner, graphs)
+    return m, probs, fr, srcs
+
+
+def warm_up(probs, opts):
+    """Set-up, tuning and graph capture of a batch shape, two iterations only (untimed)."""
+    o = solver.make_opts()
+    C.pointer(o)[0] = opts
+    o.maxit = 2
+    solver.solve_batch(probs, opts=o, raise_not_converged=False)
     torch.cuda.synchronize()
+
+
+def timed_batch(probs, opts):
     e0, e1 = _events()
     e0.record()
     us, infos = solver.solve_batch(probs, opts=opts)
     e1.record()
     torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3
+    return us, infos, e0.elapsed_time(e1) / 1e3
+
+
+def config2(order="block8", precision="mixed", freqs=None, nsrc=None, tol=1e-6, inner_tol=1e-4, warm=True):
+    """The config-2 batch (by default all 64 sources x 4 frequencies = 256 right-hand sides) in
+    one batched solve: all frequencies and sources iterate together."""
+    m, probs, fr, srcs = config2_problems(freqs, nsrc)
+    opts = solver.make_opts(tol=tol, precision=precision, order=order, inner_tol=inner_tol)
+    if warm:
+        warm_up(probs, opts)
+    us, infos, t = timed_batch(probs, opts)
     nsolve = len(fr) * len(srcs)
-    return {"workload": "config2", "solves": nsolve, "seconds": t, "solves_per_s": nsolve / t,
-            "order": order, "precision": precision, "iters": [i["iters"] for i in infos],
-            "rel_res_true_max": max(i["rel_res_true"] for i in infos), "freqs": [float(f) for f in fr],
-            "nsrc": len(srcs)}
+    out = {"workload": "config2", "solves": nsolve, "solves_per_s": nsolve / t, "order": order,
+           "precision": precision, "freqs": [float(f) for f in fr], "nsrc": len(srcs)}
+    out.update(_summary(infos, t))
+    return out, us
 
 
 def config3_problem(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cgmn"):
@@ -70,12 +104,18 @@ def config3_problem(precision="mixed", order="block8", nsrc=None, freqs=None, so
     return prob, m_true, m0
 
 
-def config3(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cgmn"):
+def config3(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cgmn", return_grad=False):
     """FWI gradient w.r.t. squared slowness: 32 jittered surface sources, 400 receivers,
     3 / 4.5 / 6 Hz on 161 x 161 x 81 (15-point PML); observed data modelled on the true
     model, gradient at the background model through the autograd function."""
     prob, m_true, m0 = config3_problem(precision, order, nsrc, freqs, solver)
     Dobs = prob.forward_model(m_true)
+    if solver == "cgmn":   # the adjoint batch's set-up, tuning and capture, untimed
+        gen = torch.Generator(device=prob.dev).manual_seed(5)
+        jobs = [S.Problem(prob.g, prob._wavenumbers(m0, float(prob.geom.freqs[k]))[0],
+                          torch.randn(len(srcs), prob.N, dtype=torch.complex128, device=prob.dev, generator=gen), 2)
+                for k, srcs in prob._units()]
+        warm_up(jobs, prob._opts())
     torch.cuda.synchronize()
     m = m0.clone().requires_grad_(True)
     prob.last_infos = []
@@ -87,20 +127,21 @@ def config3(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cg
     torch.cuda.synchronize()
     t = e0.elapsed_time(e1) / 1e3
     pairs = prob.nsrc * len(prob.geom.freqs)
-    return {"workload": "config3", "seconds": t, "grads_per_s": 1.0 / t, "pairs_per_s": pairs / t,
-            "f": float(f.item()), "grad_norm": float(m.grad.norm().item()), "order": order,
-            "precision": precision, "solver": solver, "nsrc": prob.nsrc, "freqs": [float(x) for x in prob.geom.freqs],
-            "solves": len(prob.last_infos), "iters": [i["iters"] for i in prob.last_infos],
-            "stored_wavefields": prob.wavefield_bytes() <= prob.cfg.hbm_budget_bytes}
+    out = {"workload": "config3", "seconds": t, "grads_per_s": 1.0 / t, "pairs_per_s": pairs / t,
+           "f": float(f.item()), "grad_norm": float(m.grad.norm().item()), "order": order,
+           "precision": precision, "solver": solver, "nsrc": prob.nsrc, "freqs": [float(x) for x in prob.geom.freqs],
+           "solves": len(prob.last_infos), "iters": [i["iters"] for i in prob.last_infos],
+           "stored_wavefields": prob.wavefield_bytes() <= prob.cfg.hbm_budget_bytes}
+    sw = [i for i in prob.last_infos if i.get("sweep_seconds")]
+    ss, sb = sum(i["sweep_seconds"] for i in sw), sum(i["sweep_bytes"] for i in sw)
+    out["sweep_gbs"] = sb / ss / 1e9 if ss > 0 else None
+    return (out, m.grad.detach()) if return_grad else out
 
 
-def config4(precision="mixed", order="block8", nprob=48):
-    """48 problems with seeded sizes in [64, 192] per axis, 12.5 Hz, 1-16 sources each,
-    solved in one batched call."""
-    probs_m = models.config4(nprob=nprob)
+def config4_problems(nprob=48, first=0):
+    probs_m = models.config4(nprob=first + nprob)[first:]
     dev = torch.device("cuda:0")
     probs = []
-    nsolve = 0
     for m in probs_m:
         nx, ny, _ = m.n_total
         wn = torch.as_tensor(m.wavenumber(), device=dev)
@@ -108,18 +149,42 @@ def config4(precision="mixed", order="block8", nprob=48):
         for s, (i, j, k) in enumerate(m.sources):
             b[s, int(i) + nx * int(j) + nx * ny * int(k)] = 1.0
         probs.append(solver.Problem((m.n_total, m.h, m.npml6), wn, b, 1))
-        nsolve += len(m.sources)
+    return probs_m, probs
+
+
+def config4(precision="mixed", order="block8", nprob=48, fp64_problems=None):
+    """48 problems with seeded sizes in [64, 192] per axis, 12.5 Hz, 1-16 sources each: one
+    batched solve of all of them, then (fp64_problems > 0) the first fp64_problems of them solved
+    one by one in plain FP64, the comparison the workload asks for."""
+    probs_m, probs = config4_problems(nprob)
     opts = solver.make_opts(tol=1e-6, precision=precision, order=order)
-    e0, e1 = _events()
-    e0.record()
-    us, infos = solver.solve_batch(probs, opts=opts)
-    e1.record()
-    torch.cuda.synchronize()
-    t = e0.elapsed_time(e1) / 1e3
+    warm_up(probs, opts)
+    us, infos, t = timed_batch(probs, opts)
+    nsolve = sum(len(m.sources) for m in probs_m)
     pts = sum(int(np.prod(m.n_total)) * len(m.sources) for m in probs_m)
-    return {"workload": "config4", "problems": nprob, "solves": nsolve, "seconds": t,
-            "solves_per_s": nsolve / t, "grid_points_x_rhs": pts, "order": order, "precision": precision,
-            "rel_res_true_max": max(i["rel_res_true"] for i in infos)}
+    out = {"workload": "config4", "problems": len(probs), "solves": nsolve, "solves_per_s": nsolve / t,
+           "grid_points_x_rhs": pts, "order": order, "precision": precision}
+    out.update(_summary(infos, t))
+    if fp64_problems:
+        k = min(int(fp64_problems), len(probs))
+        o64 = solver.make_opts(tol=1e-6, precision="fp64", order=order)
+        t64, n64, pts64, errs = 0.0, 0, 0, []
+        for q in range(k):
+            e0, e1 = _events()
+            e0.record()
+            u64, info64 = solver.solve(probs[q].grid, probs[q].wn, probs[q].b, opts=o64)
+            e1.record()
+            torch.cuda.synchronize()
+            t64 += e0.elapsed_time(e1) / 1e3
+            n64 += probs[q].b.shape[0]
+            pts64 += int(np.prod(probs_m[q].n_total)) * len(probs_m[q].sources)
+            d = (us[q] - u64).reshape(probs[q].b.shape[0], -1)
+            errs.append(float((d.norm(dim=1) / u64.reshape(d.shape).norm(dim=1)).max()))
+        out["fp64_one_by_one"] = {"problems": k, "solves": n64, "grid_points_x_rhs": pts64, "seconds": t64,
+                                  "solves_per_s": n64 / t64,
+                                  "mixed_batched_speedup_points_per_s": (pts / t) / (pts64 / t64),
+                                  "wavefield_rel_diff_mixed_vs_fp64_max": max(errs)}
+    return out
 
 
 def main(argv=None):
@@ -131,15 +196,17 @@ def main(argv=None):
     ap.add_argument("--freqs", type=float, nargs="*", default=None)
     ap.add_argument("--nprob", type=int, default=48)
     ap.add_argument("--solver", default="cgmn", choices=["cgmn", "mlgmres"])
+    ap.add_argument("--fp64-problems", type=int, default=0)
     a = ap.parse_args(argv)
     t0 = time.time()
     if a.config == 2:
-        out = config2(order=a.order or "block8", precision=a.precision, freqs=a.freqs, nsrc=a.nsrc)
+        out, _ = config2(order=a.order or "block8", precision=a.precision, freqs=a.freqs, nsrc=a.nsrc)
     elif a.config == 3:
         out = config3(precision=a.precision, order=a.order or "block8", nsrc=a.nsrc, freqs=a.freqs,
                       solver=a.solver)
     else:
-        out = config4(precision=a.precision, order=a.order or "block8", nprob=a.nprob)
+        out = config4(precision=a.precision, order=a.order or "block8", nprob=a.nprob,
+                      fp64_problems=a.fp64_problems)
     out["wall_s"] = time.time() - t0
     print(json.dumps(out), flush=True)
 
