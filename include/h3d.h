@@ -26,6 +26,10 @@
  *                      sequence (the (src,freq) loop of PDEfunc.m:254-347 batched: one CGMN
  *                      iteration over every column, one BLOCK8 launch per block parity over
  *                      every problem)
+ *   h3d_mex_solve      the same solve with MATLAB's host arrays (the h3d_solve_mex gateway,
+ *                      a drop-in for linearsolve(H,b,x0,mode,lsopts) on a Helmholtz operator)
+ *   h3d_fwi_grad       PDEfunc OBJ (f and g) for one frequency and a batch of sources, host
+ *                      buffers (PDEfunc.m:254-394)
  *   h3d_grad_accum     T_adj(z,u) = conj(u).*(dH'*z) summed over sources and cropped to the
  *                      physical grid (discrete_helmholtz.m:288, PDEfunc.m:386,394)
  *   h3d_src_inject,    sinc-Kaiser source injection Ps and receiver sampling Pr
@@ -255,7 +259,31 @@ int h3d_solve_host(const h3d_grid *g, const double *wn_re, const double *wn_im,
                    const void *b_host, void *u_host, int nrhs, int mode,
                    const h3d_solve_opts *opts, h3d_solve_info *info);
 
+/* H \ b (mode FORWARD) or H^H \ b (ADJOINT) with MATLAB's host arrays: what linearsolve.m:148-168
+ * with CGMN.m:36-94 computes for a Helmholtz operator, in one call (no per-iteration host round
+ * trip), behind the h3d_solve_mex gateway.  wn (N, re/im planes; im may be NULL), h[3], n[3]
+ * and npml[6] as doubles, b split planes N x nrhs (im may be NULL), u split planes N x nrhs
+ * (output).  opts NULL = h3d_default_opts.  b_rows != nx*ny*nz gives H3D_ERR_BSIZE.
+ * H3D_ERR_NOT_CONVERGED still returns the last iterate in u.  Synchronous. */
+int h3d_mex_solve(const double *wn_re, const double *wn_im, const double *h, const double *n, size_t n_len,
+                  const double *npml, const double *b_re, const double *b_im, size_t b_rows, size_t nrhs,
+                  double *u_re, double *u_im, int mode, const h3d_solve_opts *opts, h3d_solve_info *info);
+
 /* ---- FWI pieces ----------------------------------------------------------------------- */
+/* PDEfunc OBJ for one frequency and a batch of sources with host buffers (PDEfunc.m:254-394,
+ * the gradient of discrete_helmholtz.m:288): U = H \ Ps (a_s) for all sources as one batched
+ * solve, D = Pr U, f = 1/2 ||D - Dobs||_F^2 (LS_misfit.m:21-26), V = H^H \ (-Pr^T (D - Dobs)),
+ * g = sum_s Re(conj(U_s) .* (dH^H V_s)) cropped to the physical grid.  wn, dwn: N doubles, the
+ * wavenumber of this frequency on the computational grid and its derivative with respect to
+ * the model parameter (param2wavenum.m:20-49); src_pts (nsrc x 3) and rec_pts (nrec x 3):
+ * computational-grid coordinates in grid units, 0-based (as h3d_sinc_weights); src_amp: nsrc
+ * complex (re, im) pairs, the source weights w(f) Q_s prod(d)/prod(dt); dobs: nrec x nsrc complex
+ * pairs, column s at s*nrec; f: one double; g_phys: the physical grid's doubles (overwritten).
+ * opts NULL = h3d_default_opts; info (may be NULL) sums the two solves.  Synchronous. */
+int h3d_fwi_grad(const h3d_grid *g, const double *wn, const double *dwn, const double *src_pts, int nsrc,
+                 const double *src_amp, const double *rec_pts, int nrec, const double *dobs,
+                 const h3d_solve_opts *opts, double *f, double *g_phys, h3d_solve_info *info);
+
 /* g_phys[p] += scale * sum_s Re( conj(u_s[i]) * dH^H z_s [i] ) for the physical points i
  * (the PML is cropped, cut_pml=true: discrete_helmholtz.m:231-232).  dwn is the
  * derivative of the wavenumber (device, N doubles); g_phys has (nx-lo_x-hi_x) *

@@ -92,6 +92,10 @@ _SIGS = {
                                   C.POINTER(SolveInfo), vp]),
     "h3d_solve_host": (C.c_int, [C.POINTER(Grid), vp, vp, vp, vp, C.c_int, C.c_int,
                                  C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
+    "h3d_mex_solve": (C.c_int, [dp, dp, dp, dp, C.c_size_t, dp, dp, dp, C.c_size_t, C.c_size_t, dp, dp, C.c_int,
+                                C.POINTER(SolveOpts), C.POINTER(SolveInfo)]),
+    "h3d_fwi_grad": (C.c_int, [C.POINTER(Grid), dp, dp, dp, C.c_int, dp, dp, C.c_int, dp, C.POINTER(SolveOpts),
+                               dp, dp, C.POINTER(SolveInfo)]),
     "h3d_grad_accum": (C.c_int, [C.POINTER(Grid), vp, vp, vp, C.c_int, C.c_double, vp, vp]),
     "h3d_sinc_weights": (C.c_int, [C.POINTER(Grid), dp, C.c_int, C.POINTER(C.c_int32), dp]),
     "h3d_src_inject": (C.c_int, [C.POINTER(Grid), vp, vp, vp, vp, C.c_int, vp]),

@@ -47,6 +47,8 @@ MEX_VARIANTS = {
     # the band-storage gateways, install_MEX:75-86
     "Hmvp_MT_mex": ("bmvp", []),
     "sweep_MT_mex": ("bswp", []),
+    # the whole linearsolve / CGMN solve in one call (no reference binary of this name)
+    "h3d_solve_mex": ("solve", []),
 }
 
 
@@ -149,7 +151,7 @@ def build_mex(verbose: bool = False, force: bool = False) -> dict:
         if not force and _newer(so, [gw, stub_c, LIB, os.path.join(INCLUDE, "h3d.h")]):
             continue
         kflag = {"mvp": "-DH3D_GATEWAY_MVP", "swp": "-DH3D_GATEWAY_SWEEP", "bmvp": "-DH3D_GATEWAY_BAND_MVP",
-                 "bswp": "-DH3D_GATEWAY_BAND_SWEEP"}[kind]
+                 "bswp": "-DH3D_GATEWAY_BAND_SWEEP", "solve": "-DH3D_GATEWAY_SOLVE"}[kind]
         tmp = f"{so}.{os.getpid()}.tmp"
         _run([cc, "-O2", "-std=c11", "-fPIC", "-shared", kflag, *flags, "-I", INCLUDE, "-I",
               stub_dir, gw, stub_c, "-o", tmp, "-L", LIBDIR, "-lh3d",

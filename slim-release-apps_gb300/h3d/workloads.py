@@ -36,6 +36,7 @@ def _summary(infos, seconds):
             "rel_res_true_max": max(i["rel_res_true"] for i in infos),
             "sweep_gbs": (sb / ss / 1e9) if ss > 0 else None,
             "sweep_samples": sum(i["sweep_samples"] for i in infos),
+            "sweep_bytes_total": sb, "sweep_seconds_total": ss,
             "kernel_launches": int(sum(i["kernel_launches"] for i in infos))}
 
 
@@ -104,12 +105,17 @@ def config3_problem(precision="mixed", order="block8", nsrc=None, freqs=None, so
     return prob, m_true, m0
 
 
-def config3(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cgmn", return_grad=False):
+def config3(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cgmn", return_grad=False,
+            dobs_zero=False):
     """FWI gradient w.r.t. squared slowness: 32 jittered surface sources, 400 receivers,
     3 / 4.5 / 6 Hz on 161 x 161 x 81 (15-point PML); observed data modelled on the true
-    model, gradient at the background model through the autograd function."""
+    model, gradient at the background model through the autograd function.  dobs_zero: observed
+    data zero instead (no modelling run; the solves cost the same, the gradient differs)."""
     prob, m_true, m0 = config3_problem(precision, order, nsrc, freqs, solver)
-    Dobs = prob.forward_model(m_true)
+    if dobs_zero:
+        Dobs = torch.zeros(prob.nrec, prob.nsrc * len(prob.geom.freqs), dtype=torch.complex128, device=prob.dev)
+    else:
+        Dobs = prob.forward_model(m_true)
     if solver == "cgmn":   # the adjoint batch's set-up, tuning and capture, untimed
         gen = torch.Generator(device=prob.dev).manual_seed(5)
         jobs = [S.Problem(prob.g, prob._wavenumbers(m0, float(prob.geom.freqs[k]))[0],
@@ -135,6 +141,8 @@ def config3(precision="mixed", order="block8", nsrc=None, freqs=None, solver="cg
     sw = [i for i in prob.last_infos if i.get("sweep_seconds")]
     ss, sb = sum(i["sweep_seconds"] for i in sw), sum(i["sweep_bytes"] for i in sw)
     out["sweep_gbs"] = sb / ss / 1e9 if ss > 0 else None
+    out.update(sweep_bytes_total=sb, sweep_seconds_total=ss,
+               sweep_samples_total=sum(i.get("sweep_samples", 0) for i in sw))
     return (out, m.grad.detach()) if return_grad else out
 
 

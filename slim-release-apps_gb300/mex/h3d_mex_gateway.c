@@ -12,6 +12,13 @@
  *       y = Hmvp_MT_mex(coef, offset, x, nthreads)               (Hmvp_MT_mex.c:12-45)
  *   -DH3D_GATEWAY_BAND_SWEEP                           -> sweep_MT_mex (install_MEX:78-86)
  *       y = sweep_MT_mex(coef, offset, x, b, w, row_norms_sq)    (sweep_MT_mex.c:12-47)
+ *   -DH3D_GATEWAY_SOLVE                                -> h3d_solve_mex (no reference binary)
+ *       u = h3d_solve_mex(wn, h, n, npml, b, mode, tol, maxit[, precision[, stop]])
+ *       the whole linearsolve.m:148-168 + CGMN.m:36-94 solve of a Helmholtz operator
+ *       (H\b for mode 1, H'\b otherwise) in one call: precision 0 = FP64 (default), 1 =
+ *       complex64 inner solves under FP64 refinement; stop 1 = true residual (default), 0 =
+ *       CGMN.m:79's preconditioned residual.  Returns the last iterate when maxit is reached,
+ *       as CGMN.m does.
  *
  * Same argument order, same checks and error identifiers as the reference
  * gateways, same output (a new N x 1 or N x P complex double matrix).  The
@@ -144,6 +151,39 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
                                 mxGetM(B), mxGetPr(plhs[0]), mxGetPi(plhs[0]), H3D_MODE,
                                 H3D_ORDER_LEX);
     if (rc != H3D_OK) fail(rc, "Helm3dkaczswp_mex");
+}
+
+#elif defined(H3D_GATEWAY_SOLVE)
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
+{
+    (void)nlhs;
+    if (nrhs < 8) mexErrMsgIdAndTxt("h3d:badArgument", "expected (wn,h,n,npml,b,mode,tol,maxit[,precision[,stop]])");
+    const mxArray *WN = prhs[0], *H = prhs[1], *N = prhs[2], *NPML = prhs[3], *B = prhs[4];
+    const size_t nl = n_len_of(N);
+    if (nl != 3) {
+        fail(H3D_ERR_NSIZE, "h3d_solve_mex");
+        return;
+    }
+    const double *n = mxGetPr(N);
+    const size_t numel = (size_t)n[0] * (size_t)n[1] * (size_t)n[2];
+    if (mxGetM(B) != numel) {
+        fail(H3D_ERR_BSIZE, "h3d_solve_mex");
+        return;
+    }
+    h3d_solve_opts o;
+    h3d_default_opts(&o);
+    o.tol = mxGetScalar(prhs[6]);
+    o.maxit = (int32_t)mxGetScalar(prhs[7]);
+    if (nrhs > 8) o.precision = mxGetScalar(prhs[8]) != 0.0 ? H3D_PREC_MIXED : H3D_PREC_FP64;
+    if (nrhs > 9) o.stop_rule = mxGetScalar(prhs[9]) != 0.0 ? H3D_STOP_TRUE_RESIDUAL : H3D_STOP_PRECONDITIONED;
+    const int mode = mxGetScalar(prhs[5]) == 1.0 ? H3D_FORWARD : H3D_ADJOINT;   /* linearsolve.m:52-60 */
+    const size_t P = mxGetN(B);
+    plhs[0] = mxCreateDoubleMatrix(numel, P, mxCOMPLEX);
+    int rc = h3d_mex_solve(mxGetPr(WN), mxIsComplex(WN) ? mxGetPi(WN) : NULL, mxGetPr(H), n, nl, mxGetPr(NPML),
+                           mxGetPr(B), mxIsComplex(B) ? mxGetPi(B) : NULL, mxGetM(B), P, mxGetPr(plhs[0]),
+                           mxGetPi(plhs[0]), mode, &o, NULL);
+    if (rc != H3D_OK && rc != H3D_ERR_NOT_CONVERGED) fail(rc, "h3d_solve_mex");
 }
 
 #elif defined(H3D_GATEWAY_BAND_MVP) || defined(H3D_GATEWAY_BAND_SWEEP)

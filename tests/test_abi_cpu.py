@@ -141,3 +141,26 @@ def test_sinc_kaiser_restatement_against_independent_formula():
         want = np.where(np.abs(D) <= r,
                         np.sinc(D) * np.i0(beta * np.sqrt(np.clip(1 - (D / r) ** 2, 0, None))) / np.i0(beta), 0.0)
         np.testing.assert_allclose(got, want, rtol=0, atol=1e-14)
+
+
+def test_solve_gateway_and_fwi_grad_refuse_bad_sizes_before_device_work():
+    """The h3d_solve_mex gateway reports a b of the wrong height and a bad n with its own
+    Bsize / Nsize identifiers, and h3d_fwi_grad refuses missing buffers, before any device
+    call (so this runs without a GPU)."""
+    from h3d import _lib as L
+    from h3d import build
+    from oracle import mexharness as M
+
+    gw = M.MexFunction(build.build_mex()["h3d_solve_mex"])
+    n = np.array([6.0, 5.0, 4.0])
+    wn = np.ones(120)
+    with pytest.raises(M.MexError) as e:
+        gw(wn, np.ones(3), n, np.ones((2, 3)), np.ones(119), 1.0, 1e-6, 10.0)
+    assert e.value.ident == "SLIM_release_apps:tools:algorithms:ThreeDFreqModeling:h3d_solve_mex:Bsize"
+    with pytest.raises(M.MexError) as e:
+        gw(wn, np.ones(3), np.ones((2, 2)), np.ones((2, 3)), np.ones(120), 1.0, 1e-6, 10.0)
+    assert e.value.ident == "SLIM_release_apps:tools:algorithms:ThreeDFreqModeling:h3d_solve_mex:Nsize"
+    lib = L.load()
+    grid = L.make_grid((6, 5, 4), (10.0, 10.0, 10.0), 1)
+    rc = lib.h3d_fwi_grad(C.byref(grid), None, None, None, 1, None, None, 1, None, None, None, None, None)
+    assert rc == L.ERR_BAD_ARG
