@@ -179,7 +179,8 @@ int h3d_mvp(const h3d_grid *g, const void *wn_re, const void *wn_im, const void 
  * block[0] == -1 selects the kernels that form the coefficients themselves (COLOUR27: the
  * shared-memory tile kernel; BLOCK8: 12x12x12 blocks).  BLOCK8 on stored coefficients reads
  * the kernel's status word back (H3D_ERR_TIMEOUT if a bounded wait expired), so that call
- * synchronises the stream. */
+ * synchronises the stream; it runs the largest right-hand-side group the columns fill, or the
+ * configuration whose index the environment variable H3D_BLOCK8_CONFIG holds. */
 int h3d_kacz_sweep(const h3d_grid *g, const void *wn_re, const void *wn_im, double w, void *x,
                    const void *b, int nrhs, int mode, int order, const int32_t *block, int dtype,
                    void *stream);

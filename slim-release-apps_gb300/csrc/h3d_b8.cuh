@@ -35,8 +35,9 @@ struct B8Prob {
 
 // Compiled (precision, R, S) configurations of the batched kernel.
 struct B8Cfg {
-    int r;  // right-hand sides per CTA (64 r threads)
-    int s;  // depth of the coefficient ring
+    int r;    // right-hand sides per CTA
+    int rpt;  // right-hand sides per thread (64 r / rpt threads)
+    int s;    // depth of the coefficient ring
 };
 int b8_num_cfgs(bool fp64);
 B8Cfg b8_cfg(bool fp64, int c);

@@ -105,14 +105,18 @@ constexpr size_t b8_smem() { return 128 + (size_t)R * kNB * sizeof(cplx<T>) + ri
 
 // selftest != 0 (h3d_check_wait_timeout only): the first step's copies are announced on its
 // mbarrier but never issued, so that every wait of the first colour step expires.
-template <typename T, int R, int S>
-__global__ void __launch_bounds__(kNR *R) sweep_b8_kernel(const B8Prob<T> *__restrict__ probs,
-                                                          const int *__restrict__ starts, int nprob, cplx<T> *x,
-                                                          const cplx<T> *b, T w, const int *active, int par,
-                                                          int backward, int nsteps, int *err,
-                                                          unsigned long long limit_ns, int selftest)
+//
+// R right-hand sides per CTA; each thread projects one row of every colour for RPT of them,
+// from one load of the row's coefficients (64 R / RPT threads).
+template <typename T, int R, int RPT, int S>
+__global__ void __launch_bounds__(kNR *R / RPT) sweep_b8_kernel(const B8Prob<T> *__restrict__ probs,
+                                                                const int *__restrict__ starts, int nprob, cplx<T> *x,
+                                                                const cplx<T> *b, T w, const int *active, int par,
+                                                                int backward, int nsteps, int *err,
+                                                                unsigned long long limit_ns, int selftest)
 {
-    constexpr int NT = kNR * R, SLAB = 27 * kNR;
+    static_assert(R % RPT == 0, "RPT must divide R");
+    constexpr int NT = kNR * R / RPT, SLAB = 27 * kNR;
     constexpr uint32_t SLABB = slab_bytes<T>(), RVB = rinv_bytes<T>();
     extern __shared__ __align__(128) unsigned char smem[];
     __shared__ B8Prob<T> sp;
@@ -199,23 +203,30 @@ __global__ void __launch_bounds__(kNR *R) sweep_b8_kernel(const B8Prob<T> *__res
     blk_cp_async_wait_all();
     __syncthreads();
 
-    // thread slot: row (u, v, w) of every colour, right-hand side s0 + r (a half-warp spans
-    // (u, w): conflict-free box offsets, as the BLOCK8 kernel)
-    const int r = tid / kNR, row = tid % kNR;
+    // thread slot: row (u, v, w) of every colour, right-hand sides s0 + r0 .. s0 + r0 + RPT - 1
+    // (a half-warp spans (u, w): conflict-free box offsets, as the BLOCK8 kernel)
+    const int r0 = (tid / kNR) * RPT, row = tid % kNR;
     const int u = row % 4, ww = (row / 4) % 4, v = row / 16;
-    const bool mine = (act >> r) & 1u;
-    cplx<T> *bx = sx + (size_t)r * kNB;
-    const cplx<T> *bs = b ? b + sp.col0 + (s0 + r) * sp.cstride : nullptr;
-    cplx<T> bv_n = mk<T>(T(0), T(0));
+    const unsigned mine = (act >> r0) & ((1u << RPT) - 1u);
+    cplx<T> bv_n[RPT];
+#pragma unroll
+    for (int kk = 0; kk < RPT; ++kk) bv_n[kk] = mk<T>(T(0), T(0));
     auto fetch_b = [&](int q) {  // b_i of the next colour's row, one step ahead
         const int i = bi0 + q % 3 + 3 * u, j = bj0 + (q / 3) % 3 + 3 * v, k = bk0 + q / 9 + 3 * ww;
-        if (mine && i < op.nx && j < op.ny && k < op.nz) bv_n = bs[i + op.sy * j + op.sz * k];
+        if (i < op.nx && j < op.ny && k < op.nz) {
+            const long long ctr = i + op.sy * j + op.sz * k;
+#pragma unroll
+            for (int kk = 0; kk < RPT; ++kk)
+                if (mine & (1u << kk)) bv_n[kk] = b[sp.col0 + (s0 + r0 + kk) * sp.cstride + ctr];
+        }
     };
-    if (bs) fetch_b(colour_of(0));
+    if (b) fetch_b(colour_of(0));
     for (int qq = 0; qq < nsteps; ++qq) {
         const int q = colour_of(qq), buf = qq % S;
-        const cplx<T> bv = bv_n;
-        if (bs && qq + 1 < nsteps) fetch_b(colour_of(qq + 1));
+        cplx<T> bv[RPT];
+#pragma unroll
+        for (int kk = 0; kk < RPT; ++kk) bv[kk] = bv_n[kk];
+        if (b && qq + 1 < nsteps) fetch_b(colour_of(qq + 1));
         const bool ok = mbar_wait(smem_u32(bars + buf), (uint32_t)((qq / S) & 1), limit_ns);
         const int a = q % 3, bq = (q / 3) % 3, cq = q / 9;
         const int i = bi0 + a + 3 * u, j = bj0 + bq + 3 * v, k = bk0 + cq + 3 * ww;
@@ -224,12 +235,25 @@ __global__ void __launch_bounds__(kNR *R) sweep_b8_kernel(const B8Prob<T> *__res
             const int lc = (1 + a + 3 * u) + kPX * ((1 + bq + 3 * v) + kPY * (1 + cq + 3 * ww));
             if (!interior) {
                 const cplx<T> *sc = reinterpret_cast<const cplx<T> *>(ring + (size_t)buf * SLABB);
-                if (edge_block) block_row_stored<T, kPX, kPY, true>(op, bx, sc, kNR, row, bv, inv, w, i, j, k, lc);
-                else block_row_stored<T, kPX, kPY, false>(op, bx, sc, kNR, row, bv, inv, w, i, j, k, lc);
-            } else if (sp.adj) {
-                block_row<T, true, false, kPX, kPY>(op, bx, swr, nullptr, bv, inv, w, i, j, k, lc);
+                cplx<T> c[27];
+#pragma unroll
+                for (int t = 0; t < 27; ++t) c[t] = sc[t * kNR + row];
+                // neighbours outside the grid keep reading zero: a row on a face of the grid
+                // scatters to its inside neighbours only
+                uint32_t m = 0x7ffffffu;
+                if (edge_block && (i == 0 || j == 0 || k == 0 || i == op.nx - 1 || j == op.ny - 1 || k == op.nz - 1))
+                    m = inside_mask(i, j, k, op.nx, op.ny, op.nz);
+#pragma unroll
+                for (int kk = 0; kk < RPT; ++kk)
+                    if (mine & (1u << kk))
+                        row_project_c<T, kPX, kPY>(sx + (size_t)(r0 + kk) * kNB, c, m, bv[kk], inv, w, lc);
             } else {
-                block_row<T, false, false, kPX, kPY>(op, bx, swr, nullptr, bv, inv, w, i, j, k, lc);
+                T cr[27];
+                if (sp.adj) interior_coefs<T, true, kPX, kPY>(op, swr, lc, cr);
+                else interior_coefs<T, false, kPX, kPY>(op, swr, lc, cr);
+#pragma unroll
+                for (int kk = 0; kk < RPT; ++kk)
+                    if (mine & (1u << kk)) row_project_r<T, kPX, kPY>(sx + (size_t)(r0 + kk) * kNB, cr, bv[kk], inv, w, lc);
             }
         }
         if (__syncthreads_or(!ok)) {
@@ -274,12 +298,13 @@ __global__ void rinv8_kernel(const T *__restrict__ rinv, T *__restrict__ rinv8, 
     rinv8[e] = (i < nx && j < ny && k < nz) ? rinv[i + sy * j + sz * k] : T(0);
 }
 
-// Compiled configurations: complex64 R = 1, 2, 4, 8 with a 3-deep ring; complex128 R = 1, 2
-// with a 2-deep ring (the shared memory of R = 4 exceeds a CTA's 227 KB).
-const B8Cfg kCfgF32[] = {{1, 3}, {2, 3}, {4, 3}, {8, 3}};
-const B8Cfg kCfgF64[] = {{1, 2}, {2, 2}};
+// Compiled configurations (R right-hand sides per CTA, RPT per thread, ring depth S):
+// complex64 with a 3-deep ring; complex128 with a 2-deep ring (its R = 4 boxes would exceed a
+// CTA's 227 KB of shared memory).
+const B8Cfg kCfgF32[] = {{1, 1, 3}, {2, 1, 3}, {4, 1, 3}, {4, 2, 3}, {8, 1, 3}, {8, 2, 3}};
+const B8Cfg kCfgF64[] = {{1, 1, 2}, {2, 1, 2}, {2, 2, 2}};
 
-template <typename T, int R, int S>
+template <typename T, int R, int RPT, int S>
 int launch_b8(const B8Prob<T> *probs, const int *starts, int nprob, long long nctas, cplx<T> *x, const cplx<T> *b,
               T w, const int *active, int par, int backward, int nsteps, int *err, unsigned long long limit_ns,
               int selftest, cudaStream_t st)
@@ -288,11 +313,12 @@ int launch_b8(const B8Prob<T> *probs, const int *starts, int nprob, long long nc
     static_assert(smem + sizeof(B8Prob<T>) + 16 <= 232448, "batched BLOCK8 configuration exceeds shared memory");
     static bool attr_set = false;  // per instantiation and process
     if (!attr_set) {
-        H3D_CUDA_TRY(cudaFuncSetAttribute(sweep_b8_kernel<T, R, S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        H3D_CUDA_TRY(cudaFuncSetAttribute(sweep_b8_kernel<T, R, RPT, S>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)smem));
         attr_set = true;
     }
-    sweep_b8_kernel<T, R, S><<<(unsigned)nctas, kNR * R, smem, st>>>(probs, starts, nprob, x, b, w, active, par,
-                                                                     backward, nsteps, err, limit_ns, selftest);
+    sweep_b8_kernel<T, R, RPT, S><<<(unsigned)nctas, kNR * R / RPT, smem, st>>>(
+        probs, starts, nprob, x, b, w, active, par, backward, nsteps, err, limit_ns, selftest);
     return H3D_OK;
 }
 
@@ -301,21 +327,26 @@ int launch_b8_cfg(int cfg, const B8Prob<T> *probs, const int *starts, int nprob,
                   const cplx<T> *b, T w, const int *active, int par, int backward, int nsteps, int *err,
                   unsigned long long limit_ns, int selftest, cudaStream_t st)
 {
+#define H3D_B8_ARGS probs, starts, nprob, nctas, x, b, w, active, par, backward, nsteps, err, limit_ns, selftest, st
     if constexpr (sizeof(T) == 4) {
         switch (cfg) {
-        case 0: return launch_b8<T, 1, 3>(probs, starts, nprob, nctas, x, b, w, active, par, backward, nsteps, err, limit_ns, selftest, st);
-        case 1: return launch_b8<T, 2, 3>(probs, starts, nprob, nctas, x, b, w, active, par, backward, nsteps, err, limit_ns, selftest, st);
-        case 2: return launch_b8<T, 4, 3>(probs, starts, nprob, nctas, x, b, w, active, par, backward, nsteps, err, limit_ns, selftest, st);
-        case 3: return launch_b8<T, 8, 3>(probs, starts, nprob, nctas, x, b, w, active, par, backward, nsteps, err, limit_ns, selftest, st);
+        case 0: return launch_b8<T, 1, 1, 3>(H3D_B8_ARGS);
+        case 1: return launch_b8<T, 2, 1, 3>(H3D_B8_ARGS);
+        case 2: return launch_b8<T, 4, 1, 3>(H3D_B8_ARGS);
+        case 3: return launch_b8<T, 4, 2, 3>(H3D_B8_ARGS);
+        case 4: return launch_b8<T, 8, 1, 3>(H3D_B8_ARGS);
+        case 5: return launch_b8<T, 8, 2, 3>(H3D_B8_ARGS);
         default: break;
         }
     } else {
         switch (cfg) {
-        case 0: return launch_b8<T, 1, 2>(probs, starts, nprob, nctas, x, b, w, active, par, backward, nsteps, err, limit_ns, selftest, st);
-        case 1: return launch_b8<T, 2, 2>(probs, starts, nprob, nctas, x, b, w, active, par, backward, nsteps, err, limit_ns, selftest, st);
+        case 0: return launch_b8<T, 1, 1, 2>(H3D_B8_ARGS);
+        case 1: return launch_b8<T, 2, 1, 2>(H3D_B8_ARGS);
+        case 2: return launch_b8<T, 2, 2, 2>(H3D_B8_ARGS);
         default: break;
         }
     }
+#undef H3D_B8_ARGS
     set_error("batched BLOCK8 configuration %d out of range", cfg);
     return H3D_ERR_BAD_ARG;
 }

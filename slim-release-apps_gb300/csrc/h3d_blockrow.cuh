@@ -108,10 +108,11 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
 #undef H3D_CI
         // one partial sum per plane dz: three shorter dependency chains
         cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+        cplx<T> xv[27];  // kept for the scatter (the footprint is this row's alone in the colour)
 #define H3D_GI(t, dx, dy, dz)                                                                  \
     {                                                                                          \
-        const cplx<T> xv = bx[lc + dx + PX * (dy + PY * dz)];                                  \
-        fma_rc(acc[dz + 1], cr[t], xv);                                                        \
+        xv[t] = bx[lc + dx + PX * (dy + PY * dz)];                                             \
+        fma_rc(acc[dz + 1], cr[t], xv[t]);                                                     \
     }
         H3D_FOR_27(H3D_GI)
 #undef H3D_GI
@@ -119,8 +120,9 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
         const cplx<T> d = (w * inv) * (bv - atx);
 #define H3D_SI(t, dx, dy, dz)                                                                  \
     {                                                                                          \
-        cplx<T> &o = bx[lc + dx + PX * (dy + PY * dz)];                                        \
+        cplx<T> o = xv[t];                                                                     \
         fma_rc(o, cr[t], d);                                                                   \
+        bx[lc + dx + PX * (dy + PY * dz)] = o;                                                 \
     }
         H3D_FOR_27(H3D_SI)
 #undef H3D_SI
@@ -135,10 +137,11 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
 #undef H3D_CC
         const cplx<T> z = mk<T>(T(0), T(0));
         CSum<T> acc[3] = {csum_init(z), csum_init(z), csum_init(z)};
+        cplx<T> xv[27];  // kept for the scatter (the footprint is this row's alone in the colour)
 #define H3D_GC(t, dx, dy, dz)                                                                  \
     {                                                                                          \
-        const cplx<T> xv = bx[lc + dx + PX * (dy + PY * dz)];                                  \
-        csum_mac(acc[dz + 1], c[t], xv);                                                       \
+        xv[t] = bx[lc + dx + PX * (dy + PY * dz)];                                             \
+        csum_mac(acc[dz + 1], c[t], xv[t]);                                                    \
     }
         H3D_FOR_27(H3D_GC)
 #undef H3D_GC
@@ -146,8 +149,9 @@ __device__ __forceinline__ void block_row(const Op<T> &op, cplx<T> *bx, const T 
         const Scat<T> sd = scat_of((w * inv) * (bv - atx));
 #define H3D_SC(t, dx, dy, dz)                                                                  \
     if (m & (1u << t)) {                                                                       \
-        cplx<T> &o = bx[lc + dx + PX * (dy + PY * dz)];                                        \
+        cplx<T> o = xv[t];                                                                     \
         scat_mac(o, sd, c[t]);                                                                 \
+        bx[lc + dx + PX * (dy + PY * dz)] = o;                                                 \
     }
         H3D_FOR_27(H3D_SC)
 #undef H3D_SC
@@ -166,15 +170,17 @@ __device__ __forceinline__ void block_row_stored(const Op<T> &op, cplx<T> *bx, c
         const bool edge = i == 0 || j == 0 || k == 0 || i == op.nx - 1 || j == op.ny - 1 || k == op.nz - 1;
         if (edge) m = inside_mask(i, j, k, op.nx, op.ny, op.nz);
     }
-    cplx<T> c[27];
+    cplx<T> c[27], xv[27];
 #pragma unroll
     for (int t = 0; t < 27; ++t) c[t] = sc[t * NR + row];
     const cplx<T> z = mk<T>(T(0), T(0));
     CSum<T> acc[3] = {csum_init(z), csum_init(z), csum_init(z)};
+    // the gathered values stay in registers for the scatter: no other row of this colour
+    // touches the footprint, so they are still current when it is written back
 #define H3D_GS(t, dx, dy, dz)                                                                  \
     {                                                                                          \
-        const cplx<T> xv = bx[lc + dx + PX * (dy + PY * dz)];                                  \
-        csum_mac(acc[dz + 1], c[t], xv);                                                       \
+        xv[t] = bx[lc + dx + PX * (dy + PY * dz)];                                             \
+        csum_mac(acc[dz + 1], c[t], xv[t]);                                                    \
     }
     H3D_FOR_27(H3D_GS)
 #undef H3D_GS
@@ -182,11 +188,79 @@ __device__ __forceinline__ void block_row_stored(const Op<T> &op, cplx<T> *bx, c
     const Scat<T> sd = scat_of((w * inv) * (bv - atx));
 #define H3D_SS(t, dx, dy, dz)                                                                  \
     if (m & (1u << t)) {                                                                       \
-        cplx<T> &o = bx[lc + dx + PX * (dy + PY * dz)];                                        \
+        cplx<T> o = xv[t];                                                                     \
         scat_mac(o, sd, c[t]);                                                                 \
+        bx[lc + dx + PX * (dy + PY * dz)] = o;                                                 \
     }
     H3D_FOR_27(H3D_SS)
 #undef H3D_SS
+}
+
+// Row projections with the coefficients already in registers, so that one thread can project
+// the same row for several right-hand sides from one load of its coefficients.
+//   row_project_c: complex coefficients; the scatter skips the neighbours outside m
+//   row_project_r: real coefficients of an interior row (nothing outside the grid)
+// The gathered values stay in registers for the scatter (the footprint is the row's alone
+// within its colour).
+template <typename T, int PX, int PY>
+__device__ __forceinline__ void row_project_c(cplx<T> *bx, const cplx<T> (&c)[27], uint32_t m, cplx<T> bv, T inv,
+                                              T w, int lc)
+{
+    cplx<T> xv[27];
+    const cplx<T> z = mk<T>(T(0), T(0));
+    CSum<T> acc[3] = {csum_init(z), csum_init(z), csum_init(z)};
+#define H3D_GP(t, dx, dy, dz)                                                                  \
+    {                                                                                          \
+        xv[t] = bx[lc + dx + PX * (dy + PY * dz)];                                             \
+        csum_mac(acc[dz + 1], c[t], xv[t]);                                                    \
+    }
+    H3D_FOR_27(H3D_GP)
+#undef H3D_GP
+    const cplx<T> atx = cadd(cadd(csum_value(acc[0]), csum_value(acc[1])), csum_value(acc[2]));
+    const Scat<T> sd = scat_of((w * inv) * (bv - atx));
+#define H3D_SP(t, dx, dy, dz)                                                                  \
+    if (m & (1u << t)) {                                                                       \
+        cplx<T> o = xv[t];                                                                     \
+        scat_mac(o, sd, c[t]);                                                                 \
+        bx[lc + dx + PX * (dy + PY * dz)] = o;                                                 \
+    }
+    H3D_FOR_27(H3D_SP)
+#undef H3D_SP
+}
+
+template <typename T, int PX, int PY>
+__device__ __forceinline__ void row_project_r(cplx<T> *bx, const T (&cr)[27], cplx<T> bv, T inv, T w, int lc)
+{
+    cplx<T> xv[27];
+    cplx<T> acc[3] = {mk<T>(T(0), T(0)), mk<T>(T(0), T(0)), mk<T>(T(0), T(0))};
+#define H3D_GR(t, dx, dy, dz)                                                                  \
+    {                                                                                          \
+        xv[t] = bx[lc + dx + PX * (dy + PY * dz)];                                             \
+        fma_rc(acc[dz + 1], cr[t], xv[t]);                                                     \
+    }
+    H3D_FOR_27(H3D_GR)
+#undef H3D_GR
+    const cplx<T> atx = cadd(cadd(acc[0], acc[1]), acc[2]);
+    const cplx<T> d = (w * inv) * (bv - atx);
+#define H3D_SR(t, dx, dy, dz)                                                                  \
+    {                                                                                          \
+        cplx<T> o = xv[t];                                                                     \
+        fma_rc(o, cr[t], d);                                                                   \
+        bx[lc + dx + PX * (dy + PY * dz)] = o;                                                 \
+    }
+    H3D_FOR_27(H3D_SR)
+#undef H3D_SR
+}
+
+// The 27 real coefficients of an interior row (all PML values 1, real wavenumber) from the
+// wavenumber box: K_t - WM_t wn (Helm3d_27pt.h:676-825 with xi = 1).
+template <typename T, bool ADJ, int PX, int PY>
+__device__ __forceinline__ void interior_coefs(const Op<T> &op, const T *swr, int lc, T (&cr)[27])
+{
+    auto wnr = [&](int dx, int dy, int dz) { return swr[lc + dx + PX * (dy + PY * dz)]; };
+#define H3D_CIR(t, dx, dy, dz) cr[t] = coef_int<t, dx, dy, dz, T, ADJ>(op, wnr);
+    H3D_FOR_27(H3D_CIR)
+#undef H3D_CIR
 }
 
 }  // namespace h3d

@@ -1,6 +1,7 @@
 // extern "C" entry points for operator application (matvec and Kaczmarz sweep), in the
 // device-pointer form and in the MATLAB host layout used by the drop-in MEX gateway.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <vector>
 
@@ -48,6 +49,11 @@ static int kacz_sweep_t(const Op<T> &op, cplx<T> *x, const cplx<T> *b, int nrhs,
             int c = 0;  // the largest right-hand-side group the columns fill
             for (int k = 1; k < b8_num_cfgs(fp64); ++k)
                 if (b8_cfg(fp64, k).r <= nrhs) c = k;
+            // H3D_BLOCK8_CONFIG=<index> fixes the configuration (for tests of each of them)
+            if (const char *env = std::getenv("H3D_BLOCK8_CONFIG")) {
+                const int k = std::atoi(env);
+                if (k >= 0 && k < b8_num_cfgs(fp64)) c = k;
+            }
             if ((rc = batch.configure(c, st)) || (rc = batch.dsweep(x, b, w, nullptr, st))) return rc;
             int status = 0;
             H3D_CUDA_TRY(cudaMemcpyAsync(&status, batch.err, sizeof(int), cudaMemcpyDeviceToHost, st));

@@ -23,6 +23,8 @@ What is produced (all from seeded inputs, stored with the inputs):
   tolerance 1e-6): iteration count, residual history, true residual, and the solution
   at 4096 seeded indices with its 2-norm and a seeded probe product; beside it the same
   problem solved to a true residual near 1e-9 by the C oracle ("exact/").
+* ``config1_solve.npz`` -- the config-1 forward solve by the C oracle to a true residual
+  near 1e-9 (samples, norm, probe product), the FP64 reference of the bench's error figures.
 * ``config3_grad.npz`` -- PDEfunc OBJ on a reduced config-3 problem (the 161x161x81
   grid, sources 0 and 1 of the 32, all 400 receivers, 6 Hz, squared slowness at the
   background model, observed data zero), solved in the reference's row order and
@@ -34,8 +36,9 @@ What is produced (all from seeded inputs, stored with the inputs):
   (forward and adjoint bands, 2 right-hand sides).
 
 ``python tests/golden/make_golden.py band`` writes only ``band_small.npz``;
-``... config0_solve`` (about 80 s) and ``... config3_grad`` (about an hour: four
-single-threaded solves of 2.1 M unknowns, two processes) write one file each.
+``... config0_solve`` (a few minutes), ``... config1_solve`` (hours: a 4 M-unknown solve to
+1e-10, GOLDEN_THREADS threads) and ``... config3_grad`` (about an hour: four single-threaded
+solves of 2.1 M unknowns, two processes) write one file each.
 """
 from __future__ import annotations
 
@@ -175,6 +178,27 @@ def config0_solve_case(out):
     _samples(xe, out, "exact")
 
 
+def config1_solve_case(out):
+    """The config-1 forward solve (201 x 201 x 101, 20-point PML, 6 Hz, surface point source) by
+    the C oracle in FP64 to a true residual near 1e-9 (COLOUR27 row order, preconditioned
+    tolerance 1e-10, rows of a colour in parallel): the FP64 reference the bench states the
+    error of its wavefields against."""
+    from h3d import models
+    from oracle import h3d_oracle as O
+    from oracle import slim_ref
+
+    m = models.config1()
+    wn, b = m.wavenumber(), m.point_source()
+    g = O.make_grid(m.n_total, m.h, m.npml6)
+    x, hst = slim_ref.linearsolve_cgmn(g, wn, b, tol=1e-10, maxit=40000, order=O.ORDER_COLOUR27,
+                                       nthreads=int(os.environ.get("GOLDEN_THREADS", os.cpu_count())))
+    out["wn_checksum"] = np.array([np.sum(wn), np.linalg.norm(wn), wn.min(), wn.max()])
+    out["src_index"] = np.array(int(np.flatnonzero(b)[0]))
+    out["iters"] = np.array(len(hst) - 1)
+    out["rel_res_true"] = np.array(slim_ref.true_residual(g, wn, b, x))
+    _samples(x, out, "exact")
+
+
 def _config3_reduced():
     """The reduced config-3 gradient problem: sources 0 and 1 of the 32, all 400 receivers,
     6 Hz only, gradient w.r.t. squared slowness at the background model, observed data 0."""
@@ -252,6 +276,12 @@ def main():
         config0_solve_case(c0s)
         np.savez_compressed(os.path.join(HERE, "config0_solve.npz"), **c0s)
         print("wrote config0_solve.npz: iterations", int(c0s["iters"]))
+        return
+    if sys.argv[1:] == ["config1_solve"]:
+        c1: dict = {}
+        config1_solve_case(c1)
+        np.savez_compressed(os.path.join(HERE, "config1_solve.npz"), **c1)
+        print("wrote config1_solve.npz: iterations", int(c1["iters"]))
         return
     if sys.argv[1:] == ["config3_grad"]:
         c3: dict = {}

@@ -266,3 +266,28 @@ def test_mex_gateways_drop_in(cuda, golden_small):
     with pytest.raises(M.MexError) as e:
         s(gs[f"{tag}/wn"], h, n, npml, 1.5, X, B[:-2])
     assert e.value.ident == "SLIM_release_apps:tools:algorithms:ThreeDFreqModeling:Helm3dkaczswp_mex:Bsize"
+
+
+@pytest.mark.parametrize("dtype,cfg", [("c64", c) for c in range(6)] + [("c128", c) for c in range(3)])
+def test_block8_batched_kernel_configurations_match_oracle(cuda, dtype, cfg, monkeypatch):
+    """Every compiled configuration of the batched BLOCK8 kernel (right-hand sides per CTA and
+    per thread), fixed through H3D_BLOCK8_CONFIG, on nine right-hand sides (full and partly
+    filled groups) and both modes, against the C oracle's BLOCK8 sweep."""
+    import torch
+    from h3d import ops
+
+    monkeypatch.setenv("H3D_BLOCK8_CONFIG", str(cfg))
+    n, h, npml = (29, 27, 26), (25.0, 22.0, 20.0), (3, 4, 2, 3, 4, 2)
+    rng = np.random.default_rng(90 + cfg)
+    N = int(np.prod(n))
+    g = O.make_grid(n, h, npml)
+    wn = (2 * np.pi * 5.0) ** 2 / (1500.0 + 1500.0 * rng.random(N)) ** 2
+    X = rng.standard_normal((N, 9)) + 1j * rng.standard_normal((N, 9))
+    B = rng.standard_normal((N, 9)) + 1j * rng.standard_normal((N, 9))
+    cdt, rdt = (torch.complex64, np.float32) if dtype == "c64" else (torch.complex128, np.float64)
+    for mode in (1, 2):
+        ref = O.sweep(g, wn, 1.5, X, B, adj=(mode == 2), order=O.ORDER_BLOCK8, blk=(12, 12, 12), nthreads=4)
+        y = ops.kacz_sweep((n, h, npml), _t(wn.astype(rdt), cuda), 1.5, _t(X.T, cuda, cdt), _t(B.T, cuda, cdt),
+                           mode, order=3)
+        tol = 5e-5 if dtype == "c64" else 1e-12
+        assert _rel(y.cpu().numpy().T.astype(np.complex128), ref) <= tol, mode
