@@ -186,19 +186,46 @@ __global__ void __launch_bounds__(kNR *R / RPT) sweep_b8_kernel(const B8Prob<T> 
     if (tid == 0)
         for (int st = 0; st < S && st < nsteps; ++st) issue(st);
 
-    // the halo'd boxes of x (and the wavenumber box of an interior block), zero outside the grid
+    // the halo'd boxes of x (and the wavenumber box of an interior block), zero outside the grid,
+    // one box row (14 points along x) at a time.  One right-hand side: a thread per row, its 14
+    // points unrolled (fewest instructions; the 64 threads have 196 rows to copy).  Several: a
+    // half-warp per row, lane l on point l (the copies of a warp stay contiguous).
     const int i0 = bi0 - 1, j0 = bj0 - 1, k0 = bk0 - 1;
+    constexpr int kRows = kPY * (kBS + 2);
     T *swr = reinterpret_cast<T *>(ring);
-    for (int e = tid; e < kNB; e += NT) {
-        const int li = e % kPX, lj = (e / kPX) % kPY, lk = e / (kPX * kPY);
-        const int gi = i0 + li, gj = j0 + lj, gk = k0 + lk;
-        const bool in = gi >= 0 && gi < op.nx && gj >= 0 && gj < op.ny && gk >= 0 && gk < op.nz;
-        const long long g = in ? gi + op.sy * gj + op.sz * gk : 0;
-        if (interior) blk_cp_async<sizeof(T)>(swr + e, op.wn + g, in);
+    const int li_lo = max(0, -i0), li_hi = min(kPX, op.nx - i0);  // box columns inside the grid
+    if constexpr (R == 1) {
+        for (int rw = tid; rw < kRows; rw += NT) {
+            const int lj = rw % kPY, lk = rw / kPY;
+            const int gj = j0 + lj, gk = k0 + lk;
+            const bool rin = gj >= 0 && gj < op.ny && gk >= 0 && gk < op.nz;
+            const long long g0 = rin ? (long long)i0 + op.sy * gj + op.sz * gk : 0;
+            const cplx<T> *xr = x + sp.col0 + s0 * sp.cstride + g0;
 #pragma unroll
-        for (int r = 0; r < R; ++r)
-            if (act & (1u << r))
-                blk_cp_async<sizeof(cplx<T>)>(sx + (size_t)r * kNB + e, x + sp.col0 + (s0 + r) * sp.cstride + g, in);
+            for (int li = 0; li < kPX; ++li) {
+                const bool in = rin && li >= li_lo && li < li_hi;
+                if (interior) blk_cp_async<sizeof(T)>(swr + rw * kPX + li, op.wn + (in ? g0 + li : 0), in);
+                blk_cp_async<sizeof(cplx<T>)>(sx + rw * kPX + li, in ? xr + li : x, in);
+            }
+        }
+    } else {
+        constexpr int kSlots = NT / 16;
+        const int li = tid & 15, slot = tid >> 4;
+        const bool lin = li >= li_lo && li < li_hi;
+        const cplx<T> *xcol = x + sp.col0 + s0 * sp.cstride;
+        for (int rw = slot; rw < kRows; rw += kSlots) {
+            if (li >= kPX) continue;
+            const int lj = rw % kPY, lk = rw / kPY;
+            const int gj = j0 + lj, gk = k0 + lk;
+            const bool in = lin && gj >= 0 && gj < op.ny && gk >= 0 && gk < op.nz;
+            const long long g = in ? (long long)(i0 + li) + op.sy * gj + op.sz * gk : 0;
+            const int e = rw * kPX + li;
+            if (interior) blk_cp_async<sizeof(T)>(swr + e, op.wn + g, in);
+#pragma unroll
+            for (int r = 0; r < R; ++r)
+                if (act & (1u << r))
+                    blk_cp_async<sizeof(cplx<T>)>(sx + (size_t)r * kNB + e, xcol + r * sp.cstride + g, in);
+        }
     }
     blk_cp_async_wait_all();
     __syncthreads();
@@ -268,15 +295,33 @@ __global__ void __launch_bounds__(kNR *R / RPT) sweep_b8_kernel(const B8Prob<T> 
         }
         if (tid == 0 && qq + S < nsteps) issue(qq + S);  // the buffer this step used is free
     }
-    // write the box back (halo included), points inside the grid only
-    for (int e = tid; e < kNB; e += NT) {
-        const int li = e % kPX, lj = (e / kPX) % kPY, lk = e / (kPX * kPY);
-        const int gi = i0 + li, gj = j0 + lj, gk = k0 + lk;
-        if (gi < 0 || gi >= op.nx || gj < 0 || gj >= op.ny || gk < 0 || gk >= op.nz) continue;
-        const long long g = gi + op.sy * gj + op.sz * gk;
+    // write the box back (halo included), points inside the grid only, as staged
+    cplx<T> *xw = x + sp.col0 + s0 * sp.cstride;
+    if constexpr (R == 1) {
+        for (int rw = tid; rw < kRows; rw += NT) {
+            const int lj = rw % kPY, lk = rw / kPY;
+            const int gj = j0 + lj, gk = k0 + lk;
+            if (gj < 0 || gj >= op.ny || gk < 0 || gk >= op.nz) continue;
+            cplx<T> *xr = xw + (long long)i0 + op.sy * gj + op.sz * gk;
 #pragma unroll
-        for (int rr = 0; rr < R; ++rr)
-            if (act & (1u << rr)) x[sp.col0 + (s0 + rr) * sp.cstride + g] = sx[(size_t)rr * kNB + e];
+            for (int li = 0; li < kPX; ++li)
+                if (li >= li_lo && li < li_hi) xr[li] = sx[rw * kPX + li];
+        }
+    } else {
+        constexpr int kSlots = NT / 16;
+        const int li = tid & 15, slot = tid >> 4;
+        if (li < kPX && li >= li_lo && li < li_hi) {
+            for (int rw = slot; rw < kRows; rw += kSlots) {
+                const int lj = rw % kPY, lk = rw / kPY;
+                const int gj = j0 + lj, gk = k0 + lk;
+                if (gj < 0 || gj >= op.ny || gk < 0 || gk >= op.nz) continue;
+                const long long g = (long long)(i0 + li) + op.sy * gj + op.sz * gk;
+                const int e = rw * kPX + li;
+#pragma unroll
+                for (int rr = 0; rr < R; ++rr)
+                    if (act & (1u << rr)) xw[rr * sp.cstride + g] = sx[(size_t)rr * kNB + e];
+            }
+        }
     }
 }
 
