@@ -15,6 +15,8 @@ Reported (one JSON line on rank 0):
              over their device time, sampled live inside the timed solves by event nodes in the
              solver's CUDA graph
   fp64       the same solve in plain FP64 (mixed-versus-FP64 speed-up, wavefield difference)
+  error_vs_fp64_oracle  both wavefields against the C oracle's FP64 solution of the same
+             problem to a true residual of 1.1e-9 (tests/golden/config1_solve.npz)
   batched    the 256-right-hand-side batch (64 surface sources x 3/4/5/6 Hz, Ricker weights)
              as one batched mixed solve with its sweep's live roofline, beside plain FP64 solves
              of a sample of it (speed-up per solve, wavefield difference on the sample)
@@ -442,7 +444,25 @@ def run_gpu_arm(args, world, rank):
         fp64 = {"solves_per_s": 1.0 / t64, "ms_per_solve": 1e3 * t64, "iters": info64["iters"],
                 "mixed_speedup": (1.0 / (elapsed / args.steps)) / (1.0 / t64),
                 "wavefield_rel_diff_mixed_vs_fp64": diff, "rel_res_true": info64["rel_res_true"]}
-        del u64
+    else:
+        u64 = None
+    # error of the wavefields against the FP64 oracle's solution of the same problem (true
+    # residual 1.1e-9, tests/golden/config1_solve.npz)
+    oracle_err = None
+    gpath = os.path.join(ROOT, "tests", "golden", "config1_solve.npz")
+    if os.path.exists(gpath):
+        import numpy as np
+
+        d = dict(np.load(gpath))
+        idx = d["exact/idx"]
+        ref = d["exact/samples"]
+        oracle_err = {"oracle": "C oracle, COLOUR27 order, true residual %.1e" % float(d["rel_res_true"])}
+        for tag, uu in (("mixed", u), ("fp64", u64 if fp64 is not None else None)):
+            if uu is None:
+                continue
+            v = uu.reshape(-1).to(torch.complex128).cpu().numpy()
+            oracle_err[tag] = {"samples": float(np.linalg.norm(v[idx] - ref) / np.linalg.norm(ref)),
+                               "norm": abs(float(np.linalg.norm(v)) - float(d["exact/norm"])) / float(d["exact/norm"])}
     # roofline of the dominant kernel: the complex64 sweep, sampled live
     sb = sum(i["sweep_bytes"] for i in infos)
     ss = sum(i["sweep_seconds"] for i in infos)
@@ -470,8 +490,9 @@ def run_gpu_arm(args, world, rank):
                    "outer": infos[-1]["outer"], "rel_res_true": infos[-1]["rel_res_true"]},
         "e2e": {"value": e2e, "unit": "solves/s", "h2d_bytes_per_step": 24 * N, "d2h_bytes_per_step": 16 * N},
         "roofline": roof, "cpu_baseline": cpu, "gpu_launches": launches, "clocks": clocks, "fp64": fp64,
+        "error_vs_fp64_oracle": oracle_err,
     }
-    del u
+    del u, u64
     torch.cuda.empty_cache()
     if not args.skip_batched:
         line["batched"] = run_batched(args)

@@ -106,3 +106,23 @@ def test_config3_reduced_gradient_matches_oracle_golden(cuda, precision):
     print(f"config3 reduced {precision}: f {e_f:.3e}, g samples {e_s:.3e}, g norm {e_n:.3e}")
     # measured on a GB300: f 2.4e-6, g samples 6.7e-5, g norm 1.7e-6 (both precisions)
     assert e_f <= 2e-5 and e_s <= 5e-4 and e_n <= 2e-5, (e_f, e_s, e_n)
+
+
+@pytest.mark.parametrize("precision", ["mixed", "fp64"])
+def test_config1_solve_matches_fp64_oracle(cuda, precision):
+    """Config 1 (201 x 201 x 101, 20-point PML, 6 Hz, surface source), BLOCK8 to a true residual
+    of 1e-6, against the C oracle's FP64 solution to a true residual of 1.1e-9 (COLOUR27 order,
+    tests/golden/config1_solve.npz)."""
+    import torch
+    from h3d import models, solver
+
+    d = dict(np.load(os.path.join(GOLDEN, "config1_solve.npz")))
+    m = models.config1()
+    wn = m.wavenumber()
+    np.testing.assert_allclose([np.sum(wn), np.linalg.norm(wn), wn.min(), wn.max()], d["wn_checksum"], rtol=1e-12)
+    u, info = solver.solve((m.n_total, m.h, m.npml6), torch.as_tensor(wn, device=cuda),
+                           torch.as_tensor(m.point_source(), device=cuda), tol=1e-6, precision=precision)
+    assert info["converged"] == 1
+    e_s, e_n, e_p = _compare(u.cpu().numpy(), d, "exact")
+    print(f"config1 {precision}: error against the FP64 oracle {e_s:.3e} (samples), {e_n:.3e} (norm), {e_p:.3e} (probe)")
+    assert max(e_s, e_n, e_p) <= 2e-4, (e_s, e_n, e_p)
