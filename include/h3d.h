@@ -122,7 +122,9 @@ typedef struct h3d_solve_opts {
     int32_t order;          /* h3d_order, default BLOCK8 */
     int32_t stop_rule;      /* h3d_stop_rule */
     int32_t check_every;    /* iterations between host-visible convergence checks (graph length) */
-    double inner_tol;       /* MIXED: relative tolerance of each complex64 inner solve */
+    double inner_tol;       /* MIXED: relative tolerance of the first complex64 inner solve; a
+                               later one aims at half the reduction still needed (tol over the
+                               current true residual), between inner_tol and 0.1 */
     int32_t max_outer;      /* MIXED: maximum refinement steps */
     int32_t block[3];       /* BLOCK / BLOCK8 orders: block size (0 = choose automatically) */
     int32_t use_graphs;     /* capture the iteration in a CUDA graph (1) or launch eagerly (0) */

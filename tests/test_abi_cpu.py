@@ -164,3 +164,12 @@ def test_solve_gateway_and_fwi_grad_refuse_bad_sizes_before_device_work():
     grid = L.make_grid((6, 5, 4), (10.0, 10.0, 10.0), 1)
     rc = lib.h3d_fwi_grad(C.byref(grid), None, None, None, 1, None, None, 1, None, None, None, None, None)
     assert rc == L.ERR_BAD_ARG
+
+
+def test_wait_timeout_check_refuses_bad_limits_without_a_gpu():
+    """h3d_check_wait_timeout checks its limit before any device call."""
+    from h3d import _lib as L
+
+    lib = L.load()
+    for bad in (0.0, -1.0, 5000.0, float("nan")):
+        assert lib.h3d_check_wait_timeout(bad) == L.ERR_BAD_ARG
