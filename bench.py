@@ -17,6 +17,9 @@ Reported (one JSON line on rank 0):
   fp64       the same solve in plain FP64 (mixed-versus-FP64 speed-up, wavefield difference)
   error_vs_fp64_oracle  both wavefields against the C oracle's FP64 solution of the same
              problem to a true residual of 1.1e-9 (tests/golden/config1_solve.npz)
+  mlgmres    the same problem by FGMRES + the three-level ML_GMRES multigrid (the reference
+             applications' default solver; h3d_mlgmres_solve): mixed and FP64 seconds per solve,
+             outer iterations, the mixed wavefield against the oracle's
   batched    the 256-right-hand-side batch (64 surface sources x 3/4/5/6 Hz, Ricker weights)
              as one batched mixed solve with its sweep's live roofline, beside plain FP64 solves
              of a sample of it (speed-up per solve, wavefield difference on the sample)
@@ -364,6 +367,31 @@ def run_fwi(args):
     return out
 
 
+def run_mlgmres(args):
+    """Config 1 by FGMRES + ML_GMRES (the reference applications' default solver): mixed (complex64
+    V-cycle under complex128 FGMRES) and plain FP64, and the mixed wavefield against the oracle's."""
+    import numpy as np
+    import torch
+
+    from h3d import workloads as W
+
+    mixed, u = W.config1_mlgmres(precision="mixed", reps=args.mlgmres_reps, return_u=True)
+    out = {"workload": "config1 (201x201x101, 6 Hz, one source) by FGMRES (restart 5, tol 1e-6) preconditioned "
+                       "by the three-level ML_GMRES V-cycle", "mixed": mixed}
+    gpath = os.path.join(ROOT, "tests", "golden", "config1_solve.npz")
+    if os.path.exists(gpath):
+        d = dict(np.load(gpath))
+        v = u.reshape(-1).cpu().numpy()
+        out["mixed"]["error_vs_fp64_oracle_samples"] = float(
+            np.linalg.norm(v[d["exact/idx"]] - d["exact/samples"]) / np.linalg.norm(d["exact/samples"]))
+    del u
+    if not args.skip_fp64:
+        out["fp64"] = W.config1_mlgmres(precision="fp64", reps=1)
+        out["mixed_speedup"] = out["fp64"]["seconds_per_solve"] / mixed["seconds_per_solve"]
+    torch.cuda.empty_cache()
+    return out
+
+
 def run_gpu_arm(args, world, rank):
     import ctypes as C
 
@@ -494,6 +522,8 @@ def run_gpu_arm(args, world, rank):
     }
     del u, u64
     torch.cuda.empty_cache()
+    if not args.skip_mlgmres:
+        line["mlgmres"] = run_mlgmres(args)
     if not args.skip_batched:
         line["batched"] = run_batched(args)
     if not args.skip_fwi:
@@ -527,6 +557,8 @@ def main():
     ap.add_argument("--skip-fp64", action="store_true")
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
+    ap.add_argument("--skip-mlgmres", action="store_true")
+    ap.add_argument("--mlgmres-reps", type=int, default=3, help="timed config-1 FGMRES + ML_GMRES solves")
     ap.add_argument("--skip-fwi", action="store_true")
     ap.add_argument("--skip-config0", action="store_true", help="reference arm: no full config-0 CPU solve")
     ap.add_argument("--derive-ref-iters", action="store_true",

@@ -38,6 +38,8 @@
  *   h3d_axis_apply     grid transfers of the ML_GMRES multigrid preconditioner
  *                      (construct_multigrid.m:45-51, fine2coarse.m:40-55: Kronecker
  *                       products of 1D interpolation operators, one axis per call)
+ *   h3d_mlgmres_solve  linearsolve with SOLVE_FGMRES and PREC_MLGMRES (FGMRES.m, ML_GMRES.m,
+ *                      opMultigrid.m): the 3D applications' default solver
  *   h3d_band_coefs     the band-storage (mat_free = false) operator: helmholtz_3d.m:35-190
  *                      (27 x N bands of H) and conj(Htransp(H)) (opBandStorage.m:127-129)
  *   h3d_band_mvp       Hmvp_MT_mex (Hmvp_MT_mex.c:53-73, via Hmvp.m / opBandStorage.multiply)
@@ -320,6 +322,67 @@ int h3d_rec_spread(const h3d_grid *g, const int32_t *base, const double *w, int 
  * (dtype C128 or C64; the sums are formed in double). */
 int h3d_axis_apply(const int32_t *rowptr, const int32_t *col, const double *val, int n_out, int axis,
                    const int32_t dims_in[3], const void *x, void *y, int nrhs, int dtype, void *stream);
+
+/* ---- FGMRES with the ML_GMRES multigrid preconditioner -------------------------------- */
+/* One level of the hierarchy (construct_multigrid.m:10-60): its computational grid and real
+ * wavenumber on the device, in double and (for a complex64 cycle) rounded to float. */
+typedef struct h3d_ml_level {
+    h3d_grid grid;
+    const double *wn;       /* device, N values */
+    const float *wn32;      /* device, N values; may be NULL when precision is FP64 */
+} h3d_ml_level;
+
+/* A grid transfer between neighbouring levels: scale * (A_z (x) A_y (x) A_x) on fields with
+ * x fastest, each A_a an n_out[a] x n_in[a] CSR matrix on the device (h3d_axis_apply's
+ * layout).  Restriction maps level i to i+1, prolongation level i+1 to i. */
+typedef struct h3d_ml_transfer {
+    const int32_t *rowptr[3];
+    const int32_t *col[3];
+    const double *val[3];
+    int32_t n_in[3];
+    int32_t n_out[3];
+    double scale;
+} h3d_ml_transfer;
+
+typedef enum { H3D_ML_PREC_NONE = 0, H3D_ML_PREC_MLGMRES = 1 } h3d_ml_prec;
+
+typedef struct h3d_ml_opts {
+    double tol;             /* outer FGMRES relative tolerance (default 1e-6) */
+    int32_t maxit;          /* outer restart cycles (default 10000) */
+    int32_t maxinnerit;     /* outer steps per cycle (default 5), at most 16 */
+    int32_t precond;        /* h3d_ml_prec (default MLGMRES) */
+    int32_t precision;      /* h3d_precision: FP64, or MIXED = complex64 V-cycle (default FP64) */
+    int32_t k[4];           /* ML_GMRES.m:36-47 opts.k: smoother cycles and steps, coarse
+                               solver cycles and steps (default 3, 5, 3, 5; steps <= 16) */
+    double smooth_tol;      /* smoother tolerance (ML_GMRES.m:56, default 1e-6) */
+    double coarse_tol;      /* coarse solver tolerance (ML_GMRES.m:40, default 0.5) */
+} h3d_ml_opts;
+
+typedef struct h3d_ml_info {
+    int32_t iters;          /* outer FGMRES steps (quasi-residuals recorded after the leading 1) */
+    int32_t converged;      /* quasi-residual or true residual reached tol */
+    double rel_res;         /* last outer quasi-residual ratio */
+    double seconds;         /* wall time of the call (host clock, after stream sync) */
+    int64_t kernel_launches;/* device kernels the call launched */
+    int64_t host_syncs;     /* stream synchronisations the control flow needed */
+} h3d_ml_info;
+
+void h3d_ml_default_opts(h3d_ml_opts *opts);
+
+/* x = H \ b (mode FORWARD) or H^H \ b (ADJOINT) by FGMRES (FGMRES.m:33-129) preconditioned by
+ * the recursive ML_GMRES V-cycle over `nlevels` levels (ML_GMRES.m:36-72, opMultigrid.m;
+ * linearsolve.m:139-141 with discrete_helmholtz.m:349-350), or by nothing (PREC_NONE: plain
+ * restarted FGMRES = GMRES(m) on level 0).  restrict_ops / prolong_ops: nlevels - 1 transfers
+ * each.  b, x: device, complex128, level-0 size; x is the initial guess (all zeros = none) and
+ * is overwritten.  hst (optional, hst_cap doubles): the quasi-residual history, leading 1
+ * included; the call fails with H3D_ERR_BAD_ARG if it would overflow.  The control flow runs
+ * on the host; the Arnoldi steps, Givens rotations and stopping tests on the device, so that
+ * the host waits only before a step that applies the preconditioner and at the end of an
+ * unpreconditioned cycle.  Synchronises `stream` before returning. */
+int h3d_mlgmres_solve(const h3d_ml_level *levels, int nlevels, const h3d_ml_transfer *restrict_ops,
+                      const h3d_ml_transfer *prolong_ops, const void *b, void *x, int mode,
+                      const h3d_ml_opts *opts, double *hst, int hst_cap, h3d_ml_info *info,
+                      void *stream);
 
 /* ---- band storage (the reference's mat_free = false path) ---------------------------- */
 /* A band matrix holds ndiags couplings per row: coef[k + ndiags*i] = A(i, i + offsets[k])

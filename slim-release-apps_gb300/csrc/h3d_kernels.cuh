@@ -85,4 +85,10 @@ int num_block8_cfgs();
 void block8_cfg_dims(int c, int32_t *blk, int *r);
 size_t block8_cfg_smem(int c, bool fp64, bool wnc);
 
+// h3d_interp.cu: y = scale * A x along one axis (A in CSR form), or y += that (accum).
+template <typename T>
+int launch_axis(const int32_t *rowptr, const int32_t *col, const double *val, int n_out, int axis,
+                const int32_t dims_in[3], const cplx<T> *x, cplx<T> *y, int nrhs, double scale, bool accum,
+                cudaStream_t st);
+
 }  // namespace h3d

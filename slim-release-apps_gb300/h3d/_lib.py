@@ -57,6 +57,38 @@ class Problem(C.Structure):
     ]
 
 
+class MLLevel(C.Structure):
+    _fields_ = [("grid", Grid), ("wn", C.c_void_p), ("wn32", C.c_void_p)]
+
+
+class MLTransfer(C.Structure):
+    _fields_ = [
+        ("rowptr", C.c_void_p * 3), ("col", C.c_void_p * 3), ("val", C.c_void_p * 3),
+        ("n_in", C.c_int32 * 3), ("n_out", C.c_int32 * 3), ("scale", C.c_double),
+    ]
+
+
+class MLOpts(C.Structure):
+    _fields_ = [
+        ("tol", C.c_double), ("maxit", C.c_int32), ("maxinnerit", C.c_int32), ("precond", C.c_int32),
+        ("precision", C.c_int32), ("k", C.c_int32 * 4), ("smooth_tol", C.c_double),
+        ("coarse_tol", C.c_double),
+    ]
+
+
+class MLInfo(C.Structure):
+    _fields_ = [
+        ("iters", C.c_int32), ("converged", C.c_int32), ("rel_res", C.c_double), ("seconds", C.c_double),
+        ("kernel_launches", C.c_int64), ("host_syncs", C.c_int64),
+    ]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+ML_PREC_NONE, ML_PREC_MLGMRES = 0, 1
+
+
 class H3DError(RuntimeError):
     """A non-zero status from the C ABI; ``.status`` and ``.ident`` as the reference's IDs."""
 
@@ -104,6 +136,9 @@ _SIGS = {
                                  vp]),
     "h3d_axis_apply": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.POINTER(C.c_int32), vp, vp, C.c_int,
                                  C.c_int, vp]),
+    "h3d_ml_default_opts": (None, [C.POINTER(MLOpts)]),
+    "h3d_mlgmres_solve": (C.c_int, [C.POINTER(MLLevel), C.c_int, C.POINTER(MLTransfer), C.POINTER(MLTransfer),
+                                    vp, vp, C.c_int, C.POINTER(MLOpts), dp, C.c_int, C.POINTER(MLInfo), vp]),
     "h3d_band_coefs": (C.c_int, [C.POINTER(Grid), vp, vp, C.c_int, vp, C.POINTER(C.c_int64), C.c_int, vp]),
     "h3d_band_mvp": (C.c_int, [vp, C.POINTER(C.c_int64), C.c_int, C.c_int64, vp, vp, C.c_int, C.c_int, vp]),
     "h3d_band_sweep": (C.c_int, [C.POINTER(Grid), vp, C.POINTER(C.c_int64), vp, C.c_double, vp, vp, C.c_int,

@@ -15,10 +15,10 @@ after 5 steps) preconditioned by ML_GMRES (fwi_exp.m:58-62, discrete_helmholtz.m
                (ML_GMRES.m:36-72, opMultigrid.m construct with recursive_v_cycle)
   outer        FGMRES.m, preconditioned by the level-0 V-cycle
 
-Matrix-vector products are the library's 27-point kernels (h3d_mvp), the grid transfers
-its axis kernel (h3d_axis_apply); vectors live on the device, the small Hessenberg
-least-squares problems on the host.  Model coarsening and interpolation weights are set-up
-work on the host.
+The solve itself is one library call (h3d_mlgmres_solve): the FGMRES control flow in C++,
+every Arnoldi step, Givens rotation and stopping test on the device, the library's 27-point
+matvec and its axis kernel for the grid transfers.  Model coarsening and interpolation
+weights are set-up work on the host (this module).
 """
 from __future__ import annotations
 
@@ -188,109 +188,68 @@ def build_levels(v_phys, dt, npml, freq, unit="m/s", nlevels=3, device=None):
     return lv, R, P
 
 
-# ---- FGMRES.m --------------------------------------------------------------------------------
-def fgmres(A, b: torch.Tensor, x: torch.Tensor | None, tol=1e-6, maxit=math.inf, maxinnerit=10,
-           precond=None):
-    """Flexible GMRES restarted every maxinnerit steps (FGMRES.m:27-129).  Returns
-    (x, res, hst): the solution, true residual norms after each restart and the relative
-    quasi-residual history."""
-    if x is None or not bool(torch.any(x != 0)):
-        r = b.clone()
-        x = torch.zeros_like(b)
-    else:
-        r = b - A(x)
-    it = 1
-    normr0 = float(torch.linalg.vector_norm(r))
-    hst, res = [1.0], []
-    m = maxinnerit
-    if normr0 == 0.0:
-        return x, res, hst
-    while hst[-1] > tol and math.floor(it / m) < maxit:
-        beta = float(torch.linalg.vector_norm(r))
-        V = torch.empty((m, b.numel()), dtype=b.dtype, device=b.device)
-        Z = None if precond is None else torch.empty_like(V)
-        H = np.zeros((m + 1, m), complex)
-        y = np.zeros(m, complex)
-        V[0] = r / beta
-        k = 1
-        while k <= m and hst[-1] > tol:
-            if precond is None:
-                w = A(V[k - 1])
-            else:
-                Z[k - 1] = precond(V[k - 1])
-                w = A(Z[k - 1])
-            h = torch.mv(V[:k].conj(), w)                   # V(:,1:k)' w
-            w = w - torch.mv(V[:k].T, h)
-            hn = torch.linalg.vector_norm(w)
-            hh = torch.cat([h, hn.to(h.dtype).reshape(1)]).cpu().numpy()
-            H[:k, k - 1] = hh[:k]
-            H[k, k - 1] = hh[k]
-            if k < m:
-                V[k] = w / hn
-            e = np.zeros(k + 1, complex)
-            e[0] = beta
-            y[:k] = np.linalg.lstsq(H[:k + 1, :k], e, rcond=None)[0]
-            hst.append(float(np.linalg.norm(e - H[:k + 1, :k] @ y[:k]) / normr0))
-            k += 1
-            it += 1
-        yk = torch.as_tensor(y[:k - 1], device=b.device, dtype=b.dtype)
-        x = x + torch.mv((V if precond is None else Z)[:k - 1].T, yk)
-        r = b - A(x)
-        rn = float(torch.linalg.vector_norm(r))
-        if rn / normr0 < tol:
-            break
-        res.append(rn)
-    return x, res, hst
+# ---- FGMRES + ML_GMRES (h3d_mlgmres_solve) -------------------------------------------------
+def _level_structs(levels, R, P):
+    lv = (L.MLLevel * len(levels))()
+    for i, l in enumerate(levels):
+        lv[i].grid = l.grid
+        lv[i].wn = l.wn.data_ptr()
+        lv[i].wn32 = l.wn32.data_ptr()
+
+    def tr(t):
+        s = L.MLTransfer()
+        for a, op in enumerate(t.ops):
+            s.rowptr[a] = op.rowptr.data_ptr()
+            s.col[a] = op.col.data_ptr()
+            s.val[a] = op.val.data_ptr()
+            s.n_in[a] = op.n_in
+            s.n_out[a] = op.n_out
+        s.scale = float(t.scale)
+        return s
+
+    n = max(1, len(R))
+    Rs = (L.MLTransfer * n)(*[tr(t) for t in R])
+    Ps = (L.MLTransfer * n)(*[tr(t) for t in P])
+    return lv, Rs, Ps
 
 
-SMOOTH = dict(tol=1e-6, maxit=3, maxinnerit=5)
-COARSE = dict(tol=5e-1, maxit=3, maxinnerit=5)
-
-
-class MLGMRES:
-    """The recursive three-level V-cycle (opMultigrid with recursive_v_cycle)."""
-
-    def __init__(self, levels, R, P):
-        self.L, self.R, self.P = levels, R, P
-
-    def _smooth(self, i, b, x, mode):
-        return fgmres(lambda v: self.L[i].A(v, mode), b, x, **SMOOTH)[0]
-
-    def _coarse(self, i, b, mode):
-        Ai = lambda u: self.L[i].A(u, mode)
-        if i == len(self.L) - 1:
-            pre = lambda v: fgmres(Ai, v, None, **COARSE)[0]
-        else:
-            pre = lambda v: self.vcycle(i, v, mode)
-        return fgmres(Ai, b, None, precond=pre, **COARSE)[0]
-
-    def vcycle(self, i, b, mode=1):
-        x = self._smooth(i, b, None, mode)
-        r = b - self.L[i].A(x, mode)
-        xc = self._coarse(i + 1, self.R[i](r), mode)
-        x = x + self.P[i](xc)
-        return self._smooth(i, b, x, mode)
-
-    def __call__(self, b, mode=1):
-        return self.vcycle(0, b, mode)
-
-
-def solve(levels, R, P, b: torch.Tensor, tol=1e-6, maxit=10000, maxinnerit=5, mode=1, precision="fp64"):
-    """u = H \\ b by FGMRES + ML_GMRES, as linearsolve with SOLVE_FGMRES and PREC_MLGMRES.
+def solve(levels, R, P, b: torch.Tensor, tol=1e-6, maxit=10000, maxinnerit=5, mode=1, precision="fp64",
+          precond="mlgmres", x0: torch.Tensor | None = None, k=(3, 5, 3, 5), coarse_tol=0.5):
+    """u = H \\ b by FGMRES + ML_GMRES, as linearsolve with SOLVE_FGMRES and PREC_MLGMRES
+    (h3d_mlgmres_solve: the Arnoldi steps, Givens rotations and stopping tests on the device).
 
     precision "fp64": everything in complex128 (the reference's arithmetic).  "mixed": the
     outer FGMRES (its matvecs, Krylov basis and stopping test) stays complex128 and the
     V-cycle runs in complex64 -- FGMRES allows a preconditioner that changes between
     applications, so the inexact single-precision cycle only affects the iteration count.
+    precond "none": plain restarted FGMRES on level 0 (GMRES(maxinnerit)).  k: ML_GMRES.m's
+    opts.k (smoother cycles and steps, coarse-solver cycles and steps).
     Returns (u, info) with the outer iteration count and the quasi-residual history."""
-    T = MLGMRES(levels, R, P)
-    A0 = lambda v: levels[0].A(v, mode)
-    if precision == "fp64":
-        pre = lambda v: T(v, mode)
-    elif precision == "mixed":
-        pre = lambda v: T(v.to(torch.complex64), mode).to(torch.complex128)
-    else:
+    if precision not in ("fp64", "mixed"):
         raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
-    u, res, hst = fgmres(A0, b.to(torch.complex128), None, tol=tol, maxit=maxit, maxinnerit=maxinnerit,
-                         precond=pre)
-    return u, {"iters": len(hst) - 1, "hst": hst, "res": res}
+    if precond not in ("mlgmres", "none"):
+        raise ValueError(f"precond must be 'mlgmres' or 'none', not {precond!r}")
+    lib = L.load()
+    b = b.to(torch.complex128).contiguous()
+    u = torch.zeros_like(b) if x0 is None else x0.to(torch.complex128).clone().contiguous()
+    lv, Rs, Ps = _level_structs(levels, R, P)
+    o = L.MLOpts()
+    lib.h3d_ml_default_opts(C.byref(o))
+    o.tol = float(tol)
+    o.maxit = int(min(maxit, 2 ** 31 - 1))
+    o.maxinnerit = int(maxinnerit)
+    o.precond = L.ML_PREC_MLGMRES if precond == "mlgmres" else L.ML_PREC_NONE
+    o.precision = L.PREC_FP64 if precision == "fp64" else L.PREC_MIXED
+    for i in range(4):
+        o.k[i] = int(k[i])
+    o.coarse_tol = float(coarse_tol)
+    hst = np.zeros(1 + o.maxit * o.maxinnerit)
+    info = L.MLInfo()
+    st = torch.cuda.current_stream(b.device).cuda_stream
+    rc = lib.h3d_mlgmres_solve(lv, len(levels), Rs, Ps, C.c_void_p(b.data_ptr()), C.c_void_p(u.data_ptr()),
+                               ops._mode(mode), C.byref(o), hst.ctypes.data_as(L.dp), int(hst.size),
+                               C.byref(info), C.c_void_p(st))
+    L.check(rc, "h3d_mlgmres_solve")
+    d = info.as_dict()
+    d["hst"] = hst[: info.iters + 1].tolist()
+    return u, d

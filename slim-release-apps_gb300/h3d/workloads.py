@@ -3,10 +3,12 @@
     python -m h3d.workloads --config 2     # 64 sources x 4 frequencies, batched solves
     python -m h3d.workloads --config 3     # FWI gradient, 32 sources x 3 frequencies
     python -m h3d.workloads --config 4     # 48 uneven problems in one batched call
+    python -m h3d.workloads --config 1 --solver mlgmres   # config 1 by FGMRES + ML_GMRES
 
 Each prints one JSON line: throughput (solves/s or gradients/s) with CUDA-event timing on
 the launching stream, iteration counts, the worst true residual, and the solver settings.
-Config 1 (one source, the headline) is bench.py's workload.
+Config 1 (one source, the headline) by CGMN is bench.py's workload; here it runs by FGMRES with
+the ML_GMRES multigrid preconditioner (the reference applications' default solver).
 """
 from __future__ import annotations
 
@@ -195,9 +197,42 @@ def config4(precision="mixed", order="block8", nprob=48, fp64_problems=None):
     return out
 
 
+def config1_mlgmres(precision="mixed", reps=3, tol=1e-6, return_u=False):
+    """Config 1 (201 x 201 x 101 with a 20-point PML, 6 Hz, one surface source) by FGMRES +
+    ML_GMRES: seconds per solve over `reps` solves after an untimed one (CUDA events on the
+    launching stream), outer iterations, true residual, launches and host waits per solve."""
+    from . import multigrid as MG
+    from . import ops
+
+    m = models.config1()
+    dev = torch.device("cuda")
+    t0 = time.time()
+    lv, R, P = MG.build_levels(m.v, m.h, m.npml6[0], m.freq, "m/s", device=dev)
+    t_build = time.time() - t0
+    b = torch.as_tensor(m.point_source(), device=dev)
+    MG.solve(lv, R, P, b, tol=tol, precision=precision)
+    torch.cuda.synchronize()
+    e0, e1 = _events()
+    e0.record()
+    infos = []
+    for _ in range(reps):
+        u, info = MG.solve(lv, R, P, b, tol=tol, precision=precision)
+        infos.append(info)
+    e1.record()
+    torch.cuda.synchronize()
+    sec = e0.elapsed_time(e1) / 1e3 / reps
+    r = b - ops.mvp(lv[0].grid, lv[0].wn, u)
+    out = {"workload": "config1", "solver": "mlgmres", "precision": precision, "seconds_per_solve": sec,
+            "solves_per_s": 1.0 / sec, "outer_iters": infos[-1]["iters"],
+            "rel_res_true": float(r.norm() / b.norm()), "converged": infos[-1]["converged"],
+            "kernel_launches": infos[-1]["kernel_launches"], "host_syncs": infos[-1]["host_syncs"],
+            "levels": [list(l.nt) for l in lv], "level_build_s": t_build}
+    return (out, u) if return_u else out
+
+
 def main(argv=None):
     ap = argparse.ArgumentParser()
-    ap.add_argument("--config", type=int, choices=[2, 3, 4], required=True)
+    ap.add_argument("--config", type=int, choices=[1, 2, 3, 4], required=True)
     ap.add_argument("--order", default=None)
     ap.add_argument("--precision", default="mixed")
     ap.add_argument("--nsrc", type=int, default=None)
@@ -207,7 +242,11 @@ def main(argv=None):
     ap.add_argument("--fp64-problems", type=int, default=0)
     a = ap.parse_args(argv)
     t0 = time.time()
-    if a.config == 2:
+    if a.config == 1:
+        if a.solver != "mlgmres":
+            raise SystemExit("config 1 by CGMN is bench.py's workload; --config 1 takes --solver mlgmres")
+        out = config1_mlgmres(precision=a.precision)
+    elif a.config == 2:
         out, _ = config2(order=a.order or "block8", precision=a.precision, freqs=a.freqs, nsrc=a.nsrc)
     elif a.config == 3:
         out = config3(precision=a.precision, order=a.order or "block8", nsrc=a.nsrc, freqs=a.freqs,

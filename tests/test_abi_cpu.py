@@ -173,3 +173,42 @@ def test_wait_timeout_check_refuses_bad_limits_without_a_gpu():
     lib = L.load()
     for bad in (0.0, -1.0, 5000.0, float("nan")):
         assert lib.h3d_check_wait_timeout(bad) == L.ERR_BAD_ARG
+
+
+def test_mlgmres_refuses_bad_arguments_without_a_gpu():
+    """h3d_mlgmres_solve checks levels, transfers, step counts and the history buffer before
+    any device call (the level and vector pointers below are never dereferenced)."""
+    from h3d import _lib as L
+
+    lib = L.load()
+    o = L.MLOpts()
+    lib.h3d_ml_default_opts(C.byref(o))
+    assert (o.tol, o.maxit, o.maxinnerit, list(o.k), o.smooth_tol, o.coarse_tol) == \
+        (1e-6, 10000, 5, [3, 5, 3, 5], 1e-6, 0.5)                 # ML_GMRES.m:36-40,56, FGMRES.m
+    g = L.make_grid((8, 8, 8), (10.0, 10.0, 10.0), 2)
+    lv = (L.MLLevel * 2)()
+    for lvl in lv:
+        lvl.grid = g
+        lvl.wn = 256
+        lvl.wn32 = 256
+    tr = (L.MLTransfer * 1)()
+    dummy = C.c_void_p(256)
+
+    def call(nl, opts, hst=None, cap=0):
+        return lib.h3d_mlgmres_solve(lv, nl, tr, tr, dummy, dummy, L.FORWARD, C.byref(opts), hst, cap, None, None)
+
+    assert call(1, o) == L.ERR_BAD_ARG                 # the V-cycle needs two levels
+    assert call(2, o) == L.ERR_BAD_ARG                 # transfers that do not connect the grids
+    for field, bad in (("maxinnerit", 17), ("maxinnerit", 0), ("maxit", 0)):
+        o2 = L.MLOpts.from_buffer_copy(o)
+        setattr(o2, field, bad)
+        assert call(2, o2) == L.ERR_BAD_ARG
+    o3 = L.MLOpts.from_buffer_copy(o)
+    o3.k[1] = 0
+    assert call(2, o3) == L.ERR_BAD_ARG
+    o4 = L.MLOpts.from_buffer_copy(o)
+    o4.precond = L.ML_PREC_NONE
+    o4.maxit = 2
+    hst = np.zeros(10)
+    assert call(1, o4, hst.ctypes.data_as(L.dp), 10) == L.ERR_BAD_ARG   # 1 + 2 x 5 entries needed
+    assert b"hst holds 10" in lib.h3d_last_error()

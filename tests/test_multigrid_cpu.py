@@ -82,34 +82,24 @@ def test_library_interpolation_weights_match_oracle():
 
 def test_fgmres_restart_cycles_match_scipy_gmres():
     """FGMRES.m restarted every m steps is GMRES(m) (identity preconditioner) and, with a
-    fixed right preconditioner D, GMRES(m) on A D: the library's FGMRES (h3d.multigrid, on
-    CPU tensors here) and the oracle's equal scipy's independent GMRES after the same number
-    of restart cycles."""
-    import os
-    import sys
-
-    import torch
+    fixed right preconditioner D, GMRES(m) on A D: the oracle's restatement equals scipy's
+    independent GMRES after the same number of restart cycles (the library's device FGMRES
+    is held to the same scipy solution on the GPU)."""
     from scipy.sparse.linalg import gmres
-
-    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "slim-release-apps_gb300"))
-    from h3d import multigrid as MG
 
     rng = np.random.default_rng(3)
     n = 40
     A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n) + 2.5 * np.eye(n)
     b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
     D = np.diag(1.0 + rng.random(n))
-    At, bt, Dt = torch.as_tensor(A), torch.as_tensor(b), torch.as_tensor(D.astype(complex))
     for m, c in ((5, 3), (8, 2), (4, 6)):
         ref, _ = gmres(A, b, rtol=1e-30, atol=0.0, restart=m, maxiter=c)
-        x, _, hst = MG.fgmres(lambda v: At @ v, bt, None, tol=1e-30, maxit=c, maxinnerit=m)
         xo, _, hsto = ML.fgmres(lambda v: A @ v, b, None, tol=1e-30, maxit=c, maxinnerit=m)
-        assert np.linalg.norm(x.numpy() - ref) <= 1e-12 * np.linalg.norm(ref)
         assert np.linalg.norm(xo - ref) <= 1e-12 * np.linalg.norm(ref)
-        assert len(hst) == len(hsto) == c * m + 1
+        assert len(hsto) == c * m + 1
         yref, _ = gmres(A @ D, b, rtol=1e-30, atol=0.0, restart=m, maxiter=c)
-        x, _, _ = MG.fgmres(lambda v: At @ v, bt, None, tol=1e-30, maxit=c, maxinnerit=m, precond=lambda v: Dt @ v)
-        assert np.linalg.norm(x.numpy() - D @ yref) <= 1e-12 * np.linalg.norm(D @ yref)
+        xo, _, _ = ML.fgmres(lambda v: A @ v, b, None, tol=1e-30, maxit=c, maxinnerit=m, precond=lambda v: D @ v)
+        assert np.linalg.norm(xo - D @ yref) <= 1e-12 * np.linalg.norm(D @ yref)
 
 
 def test_library_levels_and_transfers_match_oracle():

@@ -44,7 +44,10 @@ def test_levels_and_transfers_match_oracle(cuda):
         assert np.max(np.abs(r32 - r_ref)) <= 1e-6 * np.max(np.abs(r_ref))
 
 
-def test_fgmres_ml_gmres_matches_oracle(cuda):
+@pytest.mark.parametrize("mode", [1, 2])
+def test_fgmres_ml_gmres_matches_oracle(cuda, mode):
+    """Forward (H) and adjoint (H^H) solves: the outer iteration count, the quasi-residual
+    history and the solution of the oracle's restatement."""
     import torch
     from h3d import multigrid as MG
 
@@ -53,15 +56,61 @@ def test_fgmres_ml_gmres_matches_oracle(cuda):
     b = np.zeros(lv_ref[0].N, complex)
     nx, ny, _ = lv_ref[0].nt
     b[nx // 2 + nx * (ny // 2) + nx * ny * 9] = 1.0
-    x_ref, _, hst_ref = ML.ml_gmres_solve(lv_ref, R_ref, P_ref, b, tol=1e-6)
+    x_ref, _, hst_ref = ML.ml_gmres_solve(lv_ref, R_ref, P_ref, b, tol=1e-6, mode=mode)
     lv, R, P = MG.build_levels(v, dt, npml, f, "m/s", device=cuda)
-    u, info = MG.solve(lv, R, P, torch.as_tensor(b, device=cuda), tol=1e-6)
+    u, info = MG.solve(lv, R, P, torch.as_tensor(b, device=cuda), tol=1e-6, mode=mode)
     u = u.cpu().numpy()
     assert info["iters"] == len(hst_ref) - 1
+    assert info["converged"] == 1
     np.testing.assert_allclose(info["hst"], hst_ref, rtol=1e-6, atol=1e-12)
     assert np.linalg.norm(u - x_ref) <= 1e-8 * np.linalg.norm(x_ref)
-    r = b - lv_ref[0].A(u)
+    r = b - lv_ref[0].A(u, mode)
     assert np.linalg.norm(r) / np.linalg.norm(b) <= 1e-6
+
+
+def test_plain_fgmres_restart_cycles_match_scipy_gmres(cuda):
+    """Without a preconditioner FGMRES.m is GMRES(m): after c cycles of m steps the library's
+    solution (device Arnoldi steps and Givens rotations) equals scipy's GMRES(m) on the
+    oracle's operator, and every step is recorded."""
+    import torch
+    from scipy.sparse.linalg import LinearOperator, gmres
+    from h3d import multigrid as MG
+
+    v, dt, npml, f = _model()
+    lv_ref, _, _ = ML.build_levels(v, dt, npml, f, "m/s")
+    lv, R, P = MG.build_levels(v, dt, npml, f, "m/s", device=cuda)
+    N = lv_ref[0].N
+    rng = np.random.default_rng(5)
+    b = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    A = LinearOperator((N, N), matvec=lambda x: lv_ref[0].A(x), dtype=complex)
+    for m, c in ((5, 3), (8, 2), (16, 1)):
+        ref, _ = gmres(A, b, rtol=1e-30, atol=0.0, restart=m, maxiter=c)
+        u, info = MG.solve(lv, R, P, torch.as_tensor(b, device=cuda), tol=1e-30, maxit=c, maxinnerit=m,
+                           precond="none")
+        assert info["iters"] == c * m and len(info["hst"]) == c * m + 1
+        assert np.all(np.diff(info["hst"]) <= 1e-12)          # GMRES residuals never grow in a cycle
+        assert np.linalg.norm(u.cpu().numpy() - ref) <= 1e-9 * np.linalg.norm(ref)
+
+
+def test_initial_guess_and_zero_rhs(cuda):
+    """A nonzero initial guess starts from r = b - H x0 (FGMRES.m:62-64) and the solve reduces
+    that residual by tol; b = 0 returns x = 0 at once."""
+    import torch
+    from h3d import multigrid as MG
+
+    v, dt, npml, f = _model(seed=1)
+    lv_ref, _, _ = ML.build_levels(v, dt, npml, f, "m/s")
+    lv, R, P = MG.build_levels(v, dt, npml, f, "m/s", device=cuda)
+    rng = np.random.default_rng(7)
+    N = lv_ref[0].N
+    b = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    x0 = rng.standard_normal(N) + 1j * rng.standard_normal(N)
+    u, info = MG.solve(lv, R, P, torch.as_tensor(b, device=cuda), tol=1e-6,
+                       x0=torch.as_tensor(x0, device=cuda), precision="mixed")
+    r0 = np.linalg.norm(b - lv_ref[0].A(x0))
+    assert np.linalg.norm(b - lv_ref[0].A(u.cpu().numpy())) <= 1e-6 * r0 * 1.01
+    z, info = MG.solve(lv, R, P, torch.zeros(N, dtype=torch.complex128, device=cuda))
+    assert info["iters"] == 0 and float(z.abs().max()) == 0.0
 
 
 def test_mixed_precision_cycle_converges(cuda):
