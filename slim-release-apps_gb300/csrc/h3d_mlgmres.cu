@@ -19,15 +19,16 @@
 // (FgState) in device memory.  An Arnoldi step is five launches: the matvec, the k inner
 // products V^H w (per-CTA partial sums), the orthogonalisation w -= V h fused with the final
 // sum of those partials and with ||w||^2 partials, one single-thread step that applies the
-// previous Givens rotations to the new Hessenberg column, forms the next rotation, updates the
-// rotated right-hand side and the quasi-residual and back-substitutes y, and the scaling
-// V(:,k+1) = w / ||w||.  The Givens update gives the least-squares solution and residual
-// norm of FGMRES.m:111-113 without a host round trip.  Every kernel after the matvec reads
+// previous Givens rotations to the new Hessenberg column, forms the next rotation and updates
+// the rotated right-hand side and the quasi-residual, and the scaling V(:,k+1) = w / ||w||.
+// The Givens update gives the least-squares residual norm of FGMRES.m:111-113 without a host
+// round trip; the solution y is back-substituted once per cycle, in the update of x.  Every kernel after the matvec reads
 // a flag of the state block (the step runs / the cycle runs) and returns at once when it is
 // clear, so the host enqueues a whole unpreconditioned cycle without waiting: it
 // synchronises once per cycle there, and before each step of a preconditioned instance (to
 // decide whether the expensive preconditioner runs at all).  Sums are deterministic: fixed
-// per-CTA partials, reduced in a fixed order in FP64.
+// per-thread and per-warp sums in the field's precision, then per-CTA partials and their
+// totals in FP64 in a fixed order.
 //
 // The mixed precision of the Python front end carries over: the outer FGMRES in complex128,
 // the V-cycle (all levels, smoothers and coarse solves) in complex64 with FP64 inner products.
@@ -35,7 +36,6 @@
 #include <functional>
 
 #include "h3d_kernels.cuh"
-#include "h3d_reduce.cuh"
 #include "h3d_vec.cuh"
 
 namespace h3d {
@@ -58,6 +58,9 @@ struct FgHead {                 // the part of the state the host reads
 struct FgState {
     FgHead hd;
     double hn;                  // ||w|| of the current step = H(k+1,k)
+    double rhn, rbeta;          // 1 / hn and 1 / beta (0 when the norm is 0)
+    double rnormr0;             // 1 / normr0
+    double gres;                // |g(k+1)|: the current quasi-residual norm (before / normr0)
     double cs[kMaxM];           // Givens rotations: cosines (real) ...
     cplx<double> sn[kMaxM];     // ... and sines
     cplx<double> g[kMaxM + 1];  // rotated beta e1
@@ -68,21 +71,50 @@ struct FgState {
 
 __device__ __forceinline__ bool closed(const int *gate) { return gate && *gate == 0; }
 
+// Block-wide sum of two per-thread values kept in the field's precision T: warp shuffles in T,
+// the eight per-warp results added in FP64 by thread 0 in a fixed order (valid there).  GB300
+// executes FP64 at a small fraction of its FP32 rate, so the complex64 cycle's vector kernels
+// form products and per-thread sums in FP32 (as a complex64 BLAS would) and leave FP64 to the
+// few values per CTA; the complex128 instances stay FP64 throughout.
+template <typename T>
+__device__ __forceinline__ double2 block_sum_t(T a, T b)
+{
+    __shared__ double sa[kThr / 32], sb[kThr / 32];
+    for (int o = 16; o > 0; o >>= 1) {
+        a += __shfl_down_sync(0xffffffffu, a, o);
+        b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) {
+        sa[wid] = (double)a;
+        sb[wid] = (double)b;
+    }
+    __syncthreads();
+    double x = 0.0, y = 0.0;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < kThr / 32; ++q) {
+            x += sa[q];
+            y += sb[q];
+        }
+    __syncthreads();
+    return make_double2(x, y);
+}
+
 // ---- element kernels ----------------------------------------------------------------------
 
-// r = b (x = 0 when zero_x); per-CTA partials of ||r||^2.
+// r = b (x = 0 when given); per-CTA partials of ||r||^2.
 template <typename T>
 __global__ void __launch_bounds__(kThr) fg_copy_kernel(const cplx<T> *__restrict__ b, cplx<T> *__restrict__ r,
                                                        cplx<T> *__restrict__ x, long long n, double *part)
 {
-    double s = 0.0;
+    T s = 0;
     for (long long e = blockIdx.x * (long long)kThr + threadIdx.x; e < n; e += (long long)gridDim.x * kThr) {
         const cplx<T> v = b[e];
         r[e] = v;
         if (x) x[e] = mk<T>(0, 0);
-        s += (double)v.re * v.re + (double)v.im * v.im;
+        s = fma(v.re, v.re, fma(v.im, v.im, s));
     }
-    const double2 t = block_sum2_r(s, 0.0);
+    const double2 t = block_sum_t<T>(s, T(0));
     if (threadIdx.x == 0) part[blockIdx.x] = t.x;
 }
 
@@ -92,29 +124,33 @@ __global__ void __launch_bounds__(kThr) fg_sub_kernel(const cplx<T> *__restrict_
                                                       long long n, double *part, const int *gate)
 {
     if (closed(gate)) return;
-    double s = 0.0;
+    T s = 0;
     for (long long e = blockIdx.x * (long long)kThr + threadIdx.x; e < n; e += (long long)gridDim.x * kThr) {
         const cplx<T> v = b[e] - ax[e];
         r[e] = v;
-        s += (double)v.re * v.re + (double)v.im * v.im;
+        s = fma(v.re, v.re, fma(v.im, v.im, s));
     }
     if (!part) return;
-    const double2 t = block_sum2_r(s, 0.0);
+    const double2 t = block_sum_t<T>(s, T(0));
     if (threadIdx.x == 0) part[blockIdx.x] = t.x;
 }
 
-// dst = src / *div (complex divided by a real, in the field's precision).
+// dst = src * (*rcp): V(:,k) = w / ||w|| with the reciprocal formed once per step.
 template <typename T>
 __global__ void __launch_bounds__(kThr) fg_scale_kernel(const cplx<T> *__restrict__ src, cplx<T> *__restrict__ dst,
-                                                        long long n, const double *div, const int *gate)
+                                                        long long n, const double *rcp, const int *gate)
 {
     if (closed(gate)) return;
-    const T d = (T)*div;
+    const T d = (T)*rcp;
     for (long long e = blockIdx.x * (long long)kThr + threadIdx.x; e < n; e += (long long)gridDim.x * kThr) {
         const cplx<T> v = src[e];
-        dst[e] = mk<T>(v.re / d, v.im / d);
+        dst[e] = mk<T>(v.re * d, v.im * d);
     }
 }
+
+// Element loops take kU elements per thread per pass (stride apart, each coalesced across the
+// warp) so that kU x (vectors) independent loads are in flight before the arithmetic.
+constexpr int kU = 4;
 
 // Per-CTA partials of h_j = V_j^H w, j < nv <= MV: part[j * gridDim.x + cta].
 template <typename T, int MV>
@@ -123,27 +159,49 @@ __global__ void __launch_bounds__(kThr) fg_dots_kernel(const cplx<T> *__restrict
                                                        double2 *__restrict__ part, const int *gate)
 {
     if (closed(gate)) return;
-    cplx<double> acc[MV];
+    cplx<T> acc[MV];
 #pragma unroll
-    for (int j = 0; j < MV; ++j) acc[j] = mk<double>(0, 0);
-    for (long long e = blockIdx.x * (long long)kThr + threadIdx.x; e < n; e += (long long)gridDim.x * kThr) {
-        const cplx<T> wv = w[e];
-        const cplx<double> wd = mk<double>(wv.re, wv.im);
+    for (int j = 0; j < MV; ++j) acc[j] = mk<T>(0, 0);
+    const long long stride = (long long)gridDim.x * kThr;
+    long long e = blockIdx.x * (long long)kThr + threadIdx.x;
+    for (; e + (kU - 1) * stride < n; e += kU * stride) {
+        cplx<T> wv[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) wv[u] = w[e + u * stride];
 #pragma unroll
         for (int j = 0; j < MV; ++j) {
             if (j < nv) {
-                const cplx<T> v = V[(long long)j * n + e];
-                cmac_cb(acc[j], wd, mk<double>(v.re, v.im));  // conj(v) * w
+                cplx<T> v[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) v[u] = V[(long long)j * n + e + u * stride];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) cmac_cb(acc[j], wv[u], v[u]);  // conj(v) * w
             }
         }
+    }
+    for (; e < n; e += stride) {
+        const cplx<T> wv = w[e];
+#pragma unroll
+        for (int j = 0; j < MV; ++j)
+            if (j < nv) cmac_cb(acc[j], wv, V[(long long)j * n + e]);
     }
 #pragma unroll
     for (int j = 0; j < MV; ++j) {
         if (j < nv) {
-            const double2 t = block_sum2_r(acc[j].re, acc[j].im);
+            const double2 t = block_sum_t<T>(acc[j].re, acc[j].im);
             if (threadIdx.x == 0) part[(long long)j * gridDim.x + blockIdx.x] = t;
         }
     }
+}
+
+// a -= v * h
+template <typename T>
+__device__ __forceinline__ void csub_mul(cplx<T> &a, cplx<T> v, cplx<T> h)
+{
+    a.re -= v.re * h.re;
+    a.re += v.im * h.im;
+    a.im -= v.re * h.im;
+    a.im -= v.im * h.re;
 }
 
 // w -= sum_j V_j h_j with h summed here from the dots' partials (every CTA in the same fixed
@@ -154,7 +212,7 @@ __global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict
                                                        FgState *st, double *part, const int *gate)
 {
     if (closed(gate)) return;
-    __shared__ cplx<double> sh[kMaxM];
+    __shared__ cplx<T> sh[kMaxM];
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     for (int j = wid; j < nv; j += kThr / 32) {
         double re = 0.0, im = 0.0;
@@ -168,48 +226,97 @@ __global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict
             im += __shfl_down_sync(0xffffffffu, im, o);
         }
         if (lane == 0) {
-            sh[j] = mk<double>(re, im);
-            if (blockIdx.x == 0) st->h[j] = sh[j];
+            sh[j] = mk<T>((T)re, (T)im);
+            if (blockIdx.x == 0) st->h[j] = mk<double>(re, im);
         }
     }
     __syncthreads();
-    double s = 0.0;
-    for (long long e = blockIdx.x * (long long)kThr + threadIdx.x; e < n; e += (long long)gridDim.x * kThr) {
-        const cplx<T> wv = w[e];
-        cplx<double> a = mk<double>(wv.re, wv.im);
+    T s = 0;
+    const long long stride = (long long)gridDim.x * kThr;
+    long long e = blockIdx.x * (long long)kThr + threadIdx.x;
+    for (; e + (kU - 1) * stride < n; e += kU * stride) {
+        cplx<T> a[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) a[u] = w[e + u * stride];
 #pragma unroll
         for (int j = 0; j < MV; ++j) {
             if (j < nv) {
-                const cplx<T> v = V[(long long)j * n + e];
-                const cplx<double> p = mk<double>(v.re, v.im) * sh[j];
-                a = a - p;
+                cplx<T> v[kU];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) v[u] = V[(long long)j * n + e + u * stride];
+                const cplx<T> hj = sh[j];
+#pragma unroll
+                for (int u = 0; u < kU; ++u) csub_mul(a[u], v[u], hj);
             }
         }
-        const cplx<T> o = mk<T>((T)a.re, (T)a.im);
-        w[e] = o;
-        s += (double)o.re * o.re + (double)o.im * o.im;
+#pragma unroll
+        for (int u = 0; u < kU; ++u) {
+            w[e + u * stride] = a[u];
+            s = fma(a[u].re, a[u].re, fma(a[u].im, a[u].im, s));
+        }
     }
-    const double2 t = block_sum2_r(s, 0.0);
+    for (; e < n; e += stride) {
+        cplx<T> a = w[e];
+#pragma unroll
+        for (int j = 0; j < MV; ++j)
+            if (j < nv) csub_mul(a, V[(long long)j * n + e], sh[j]);
+        w[e] = a;
+        s = fma(a.re, a.re, fma(a.im, a.im, s));
+    }
+    const double2 t = block_sum_t<T>(s, T(0));
     if (threadIdx.x == 0) part[blockIdx.x] = t.x;
 }
 
-// x += sum_{j < k} B_j y_j over the steps of the cycle (FGMRES.m:117-121).
+// x += sum_{j < k} B_j y_j over the steps of the cycle (FGMRES.m:117-121).  y = R \ g, the
+// least-squares solution of FGMRES.m:111 after the cycle's last step, is back-substituted here
+// (thread 0 of every CTA, from the rotated Hessenberg matrix) rather than after every step;
+// CTA 0 stores it in the state.
 template <typename T>
 __global__ void __launch_bounds__(kThr) fg_xupd_kernel(cplx<T> *__restrict__ x, const cplx<T> *__restrict__ B,
-                                                       long long n, const FgState *st, const int *gate)
+                                                       long long n, FgState *st, const int *gate)
 {
     if (closed(gate)) return;
-    __shared__ cplx<double> sy[kMaxM];
+    __shared__ cplx<double> sR[kMaxM * kMaxM], sg[kMaxM], sy[kMaxM];
+    __shared__ cplx<T> syt[kMaxM];
     const int kk = st->hd.k;
-    if (threadIdx.x < kMaxM) sy[threadIdx.x] = threadIdx.x < kk ? st->y[threadIdx.x] : mk<double>(0, 0);
+    for (int q = threadIdx.x; q < kk * kMaxM; q += kThr) sR[q] = st->R[q];
+    if (threadIdx.x < kk) sg[threadIdx.x] = st->g[threadIdx.x];
     __syncthreads();
-    for (long long e = blockIdx.x * (long long)kThr + threadIdx.x; e < n; e += (long long)gridDim.x * kThr) {
-        cplx<double> a = mk<double>(0, 0);
-        for (int j = 0; j < kk; ++j) {
-            const cplx<T> v = B[(long long)j * n + e];
-            a = a + mk<double>(v.re, v.im) * sy[j];
+    if (threadIdx.x == 0) {
+        for (int i = kk - 1; i >= 0; --i) {
+            cplx<double> t = sg[i];
+            for (int l = i + 1; l < kk; ++l) t = t - sR[l * kMaxM + i] * sy[l];
+            const cplx<double> d = sR[i * kMaxM + i];
+            const double dd = cabs2(d);
+            sy[i] = dd == 0.0 ? mk<double>(0, 0) : (1.0 / dd) * (t * cconj(d));
         }
-        x[e] = x[e] + mk<T>((T)a.re, (T)a.im);
+        for (int i = 0; i < kk; ++i) {
+            syt[i] = mk<T>((T)sy[i].re, (T)sy[i].im);
+            if (blockIdx.x == 0) st->y[i] = sy[i];
+        }
+    }
+    __syncthreads();
+    const long long stride = (long long)gridDim.x * kThr;
+    long long e = blockIdx.x * (long long)kThr + threadIdx.x;
+    for (; e + (kU - 1) * stride < n; e += kU * stride) {
+        cplx<T> a[kU];
+#pragma unroll
+        for (int u = 0; u < kU; ++u) a[u] = mk<T>(0, 0);
+        for (int j = 0; j < kk; ++j) {
+            cplx<T> v[kU];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) v[u] = B[(long long)j * n + e + u * stride];
+            const cplx<T> yj = syt[j];
+#pragma unroll
+            for (int u = 0; u < kU; ++u) cmac(a[u], v[u], yj);
+        }
+#pragma unroll
+        for (int u = 0; u < kU; ++u) x[e + u * stride] = x[e + u * stride] + a[u];
+    }
+    for (; e < n; e += stride) {
+        cplx<T> a = mk<T>(0, 0);
+        for (int j = 0; j < kk; ++j) cmac(a, B[(long long)j * n + e], syt[j]);
+        x[e] = x[e] + a;
     }
 }
 
@@ -228,7 +335,7 @@ __device__ double sum_parts(const double *part, int nparts)
 {
     double s = 0.0;
     for (int p = threadIdx.x; p < nparts; p += kThr) s += part[p];
-    return block_sum2_r(s, 0.0).x;
+    return block_sum_t<double>(s, 0.0).x;
 }
 
 __device__ __forceinline__ bool cycles_left(int it, int m, long long maxit)
@@ -266,70 +373,90 @@ __global__ void __launch_bounds__(kThr) fg_norm_kernel(FgState *st, const double
         }
     }
     h.beta = nr;
+    st->rbeta = nr != 0.0 ? 1.0 / nr : 0.0;
+    st->gres = nr;
+    if (first) st->rnormr0 = nr != 0.0 ? 1.0 / nr : 0.0;
     h.k = 0;
     h.go = h.live;
     st->g[0] = mk<double>(nr, 0.0);
 }
 
 // Step j of the cycle (0-based): H(1:j+1, j+1) = h, H(j+2, j+1) = ||w||; Givens rotations
-// replace the least-squares solve of FGMRES.m:111 (same solution and residual norm).
+// replace the least-squares solve of FGMRES.m:111 (same solution and residual norm; y itself
+// is back-substituted once per cycle, by fg_xupd_kernel).  With H(j+2, j+1) = ||w|| real the
+// new rotation needs only reciprocal square roots (FP64 divisions and square roots are long
+// dependent sequences on this GPU): c = |a| / r, s = (a / |a|) ||w|| / r, r = sqrt(|a|^2 +
+// ||w||^2), and the quasi-residual |g(j+2)| = |s| |g(j+1)| follows without a square root.
+// The state the step reads is copied to shared memory by all threads at once.
 // hist (optional): the quasi-residual history, hist[nhst] written after each step.
 __global__ void __launch_bounds__(kThr) fg_step_kernel(FgState *st, const double *part, int nparts, int j, int m,
                                                        double tol, double *hist, const int *gate)
 {
     if (closed(gate)) return;
-    const double hn = sqrt(sum_parts(part, nparts));
+    __shared__ cplx<double> ssn[kMaxM], sc[kMaxM + 1];
+    __shared__ double scs[kMaxM];
+    if (threadIdx.x < j) {
+        scs[threadIdx.x] = st->cs[threadIdx.x];
+        ssn[threadIdx.x] = st->sn[threadIdx.x];
+    }
+    if (threadIdx.x <= j) sc[threadIdx.x] = st->h[threadIdx.x];
+    const double w2 = sum_parts(part, nparts);  // ||w||^2 (synchronises the block)
     if (threadIdx.x != 0) return;
-    cplx<double> c[kMaxM + 1];
-    for (int i = 0; i <= j; ++i) c[i] = st->h[i];
-    c[j + 1] = mk<double>(hn, 0.0);
+    const cplx<double> gj = st->g[j];
+    const double gres = st->gres;
+    FgHead &h = st->hd;
+    const double rnormr0 = st->rnormr0;
+    const double rhn = w2 > 0.0 ? rsqrt(w2) : 0.0;
+    const double hn = w2 * rhn;
+    cplx<double> *c = sc;
+    // rotations 0..j-1 on the column (c[i + 1] is the unrotated h[i + 1] for i + 1 <= j)
     for (int i = 0; i < j; ++i) {
-        const double ci = st->cs[i];
-        const cplx<double> si = st->sn[i];
+        const double ci = scs[i];
+        const cplx<double> si = ssn[i];
         const cplx<double> t = ci * c[i] + si * c[i + 1];
         c[i + 1] = ci * c[i + 1] - cconj(si) * c[i];
         c[i] = t;
     }
-    const cplx<double> a = c[j], bb = c[j + 1];
-    const double na = sqrt(cabs2(a)), nb = sqrt(cabs2(bb));
-    double cj;
-    cplx<double> sj;
-    if (nb == 0.0) {
+    const cplx<double> a = c[j];
+    const double na2 = cabs2(a);
+    double cj, sabs;
+    cplx<double> sj, rjj;
+    if (w2 == 0.0) {
         cj = 1.0;
         sj = mk<double>(0, 0);
-    } else if (na == 0.0) {
+        sabs = 0.0;
+        rjj = a;
+    } else if (na2 == 0.0) {
         cj = 0.0;
-        sj = (1.0 / nb) * cconj(bb);
-        c[j] = mk<double>(nb, 0.0);
+        sj = mk<double>(1.0, 0.0);
+        sabs = 1.0;
+        rjj = mk<double>(hn, 0.0);
     } else {
-        const double r = hypot(na, nb);
-        const cplx<double> ph = (1.0 / na) * a;
-        cj = na / r;
-        sj = (1.0 / r) * (ph * cconj(bb));
-        c[j] = r * ph;
+        const double r2 = na2 + w2, rr = rsqrt(r2), rna = rsqrt(na2);
+        const cplx<double> ph = rna * a;
+        cj = na2 * rna * rr;
+        sabs = hn * rr;
+        sj = sabs * ph;
+        rjj = (r2 * rr) * ph;
     }
+    c[j] = rjj;
     st->cs[j] = cj;
     st->sn[j] = sj;
     for (int i = 0; i <= j; ++i) st->R[j * kMaxM + i] = c[i];
-    const cplx<double> gj = st->g[j];
     st->g[j + 1] = mk<double>(0, 0) - cconj(sj) * gj;
     st->g[j] = cj * gj;
-    // y(1:j+1) = R \ g(1:j+1)
-    for (int i = j; i >= 0; --i) {
-        cplx<double> s = st->g[i];
-        for (int l = i + 1; l <= j; ++l) s = s - st->R[l * kMaxM + i] * st->y[l];
-        const cplx<double> d = st->R[i * kMaxM + i];
-        const double dd = cabs2(d);
-        st->y[i] = dd == 0.0 ? mk<double>(0, 0) : (1.0 / dd) * (s * cconj(d));
-    }
-    FgHead &h = st->hd;
-    h.hst = sqrt(cabs2(st->g[j + 1])) / h.normr0;
+    const double gnew = sabs * gres;
+    st->gres = gnew;
+    const double q = gnew * rnormr0;
+    h.hst = q;
     st->hn = hn;
-    h.nhst += 1;
-    if (hist) hist[h.nhst] = h.hst;
+    st->rhn = rhn;
+    const int nh = h.nhst + 1;
+    h.nhst = nh;
+    if (hist) hist[nh] = q;
     h.it += 1;
     h.k = j + 1;
-    h.go = (h.hst > tol && j + 1 < m) ? 1 : 0;
+    h.go = (q > tol && j + 1 < m) ? 1 : 0;
 }
 
 // ---- host side -------------------------------------------------------------------------------
@@ -349,9 +476,12 @@ int device_sms()
     return sms;
 }
 
+// CTAs of the reduction kernels (and entries of the partial-sum buffers): one pass of kU
+// elements per thread on the coarse levels (latency-bound there: more CTAs in flight), at most
+// four CTAs per SM.
 int parts_for(long long n)
 {
-    const long long p = (n + 2047) / 2048;
+    const long long p = (n + kU * kThr - 1) / (kU * kThr);
     const long long cap = 4LL * device_sms();
     return (int)(p < 1 ? 1 : (p > cap ? cap : p));
 }
@@ -450,7 +580,7 @@ int fgmres(Run &R, Fg<T> &I, const Op<T> &op, const cplx<T> *b, cplx<T> *x, bool
             if ((rc = R.fetch(I.st))) return rc;
             if (!R.hh->live) break;
         }
-        H3D_ML_LAUNCH((fg_scale_kernel<T><<<nb, kThr, 0, R.s>>>(I.r, I.V, n, &I.st->hd.beta, live)));
+        H3D_ML_LAUNCH((fg_scale_kernel<T><<<nb, kThr, 0, R.s>>>(I.r, I.V, n, &I.st->rbeta, live)));
         for (int j = 0; j < m; ++j) {
             const cplx<T> *vj = I.V + (long long)j * n;
             if (pre) {
@@ -464,7 +594,11 @@ int fgmres(Run &R, Fg<T> &I, const Op<T> &op, const cplx<T> *b, cplx<T> *x, bool
             }
             if ((rc = launch_mvp<T>(op, vj, I.w, 1, R.adj, false, R.s))) return rc;
             ++R.launches;
-            if (j < 8) {
+            if (j < 4) {
+                H3D_ML_LAUNCH((fg_dots_kernel<T, 4><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, go)));
+                H3D_ML_LAUNCH((fg_orth_kernel<T, 4><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, I.nparts,
+                                                                          I.st, I.part, go)));
+            } else if (j < 8) {
                 H3D_ML_LAUNCH((fg_dots_kernel<T, 8><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, go)));
                 H3D_ML_LAUNCH((fg_orth_kernel<T, 8><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, I.nparts,
                                                                           I.st, I.part, go)));
@@ -476,7 +610,7 @@ int fgmres(Run &R, Fg<T> &I, const Op<T> &op, const cplx<T> *b, cplx<T> *x, bool
             H3D_ML_LAUNCH((fg_step_kernel<<<1, kThr, 0, R.s>>>(I.st, I.part, I.nparts, j, m, tol, I.hist, go)));
             if (j + 1 < m)
                 H3D_ML_LAUNCH((fg_scale_kernel<T><<<nb, kThr, 0, R.s>>>(I.w, I.V + (long long)(j + 1) * n, n,
-                                                                        &I.st->hn, go)));
+                                                                        &I.st->rhn, go)));
         }
         H3D_ML_LAUNCH((fg_xupd_kernel<T><<<nb, kThr, 0, R.s>>>(x, basis, n, I.st, live)));
         if ((rc = launch_mvp<T>(op, x, I.w, 1, R.adj, false, R.s))) return rc;

@@ -240,12 +240,13 @@ def main(argv=None):
     ap.add_argument("--nprob", type=int, default=48)
     ap.add_argument("--solver", default="cgmn", choices=["cgmn", "mlgmres"])
     ap.add_argument("--fp64-problems", type=int, default=0)
+    ap.add_argument("--reps", type=int, default=3, help="config 1: timed solves after the untimed one")
     a = ap.parse_args(argv)
     t0 = time.time()
     if a.config == 1:
         if a.solver != "mlgmres":
             raise SystemExit("config 1 by CGMN is bench.py's workload; --config 1 takes --solver mlgmres")
-        out = config1_mlgmres(precision=a.precision)
+        out = config1_mlgmres(precision=a.precision, reps=a.reps)
     elif a.config == 2:
         out, _ = config2(order=a.order or "block8", precision=a.precision, freqs=a.freqs, nsrc=a.nsrc)
     elif a.config == 3:
