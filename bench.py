@@ -25,8 +25,10 @@ Reported (one JSON line on rank 0):
              of a sample of it (speed-up per solve, wavefield difference on the sample)
   fwi        the FWI gradient of the 161 x 161 x 81 workload (32 sources x 3 frequencies, 400
              receivers) in mixed precision, beside a plain-FP64 gradient of a sample of its
-             (source, frequency) pairs, and the error of the mixed gradient against the FP64
-             oracle's gradient on the reduced problem of tests/golden/config3_grad.npz
+             (source, frequency) pairs, the same gradient with every solve by FGMRES + ML_GMRES
+             (fwi.mlgmres, and its difference to the CGMN gradient), and the error of the mixed
+             gradient against the FP64 oracle's gradient on the reduced problem of
+             tests/golden/config3_grad.npz
   cpu_baseline  the CPU oracle port of the reference algorithm (lexicographic Kaczmarz sweep,
              single-threaded per right-hand side as the reference) timed on a bounded sample of
              CGMN iterations and extrapolated with the reference-order iteration count
@@ -335,7 +337,7 @@ def run_fwi(args):
 
     from h3d import workloads as W
 
-    mixed = W.config3(precision="mixed")
+    mixed, g_cgmn = W.config3(precision="mixed", return_grad=True)
     out = {"workload": "config3: 161x161x81 incl. 15-pt PML, 32 sources x 3/4.5/6 Hz, 400 receivers, gradient "
                        "w.r.t. squared slowness at the background model", "mixed": mixed,
            "roofline": _roofline(mixed["sweep_bytes_total"], mixed["sweep_seconds_total"],
@@ -346,6 +348,13 @@ def run_fwi(args):
         f64 = W.config3(precision="fp64", nsrc=args.fwi_fp64_nsrc, freqs=[6.0], dobs_zero=True)
         out["fp64_sample"] = {"what": f"sources 0-{args.fwi_fp64_nsrc - 1} at 6 Hz, plain FP64", **f64}
         out["mixed_speedup_pairs_per_s_lower_bound"] = mixed["pairs_per_s"] / f64["pairs_per_s"]
+    if not args.skip_fwi_mlgmres:
+        # the same gradient with every forward and adjoint solve by FGMRES + ML_GMRES (one source
+        # at a time, levels built per frequency inside the timed region)
+        ml, g_ml = W.config3(precision="mixed", solver="mlgmres", return_grad=True)
+        ml["grad_rel_diff_vs_cgmn"] = float((g_ml - g_cgmn).norm() / g_cgmn.norm())
+        out["mlgmres"] = ml
+    del g_cgmn
     path = os.path.join(ROOT, "tests", "golden", "config3_grad.npz")
     if os.path.exists(path):
         d = dict(np.load(path))
@@ -558,6 +567,7 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-mlgmres", action="store_true")
+    ap.add_argument("--skip-fwi-mlgmres", action="store_true", help="no config-3 gradient by the multigrid solver")
     ap.add_argument("--mlgmres-reps", type=int, default=3, help="timed config-1 FGMRES + ML_GMRES solves")
     ap.add_argument("--skip-fwi", action="store_true")
     ap.add_argument("--skip-config0", action="store_true", help="reference arm: no full config-0 CPU solve")

@@ -60,6 +60,7 @@ struct FgState {
     double hn;                  // ||w|| of the current step = H(k+1,k)
     double rhn, rbeta;          // 1 / hn and 1 / beta (0 when the norm is 0)
     double rnormr0;             // 1 / normr0
+    double sv[kMaxM];           // basis vector j = sv[j] x stored vector j (1 when stored normalised)
     double gres;                // |g(k+1)|: the current quasi-residual norm (before / normr0)
     double cs[kMaxM];           // Givens rotations: cosines (real) ...
     cplx<double> sn[kMaxM];     // ... and sines
@@ -153,9 +154,11 @@ __global__ void __launch_bounds__(kThr) fg_scale_kernel(const cplx<T> *__restric
 constexpr int kU = 4;
 
 // Per-CTA partials of h_j = V_j^H w, j < nv <= MV: part[j * gridDim.x + cta].
+// Stored vector 0 is u0, vector j >= 1 is V + j n (the unpreconditioned instances keep vector 0
+// in their residual buffer).
 template <typename T, int MV>
-__global__ void __launch_bounds__(kThr) fg_dots_kernel(const cplx<T> *__restrict__ V, int nv,
-                                                       const cplx<T> *__restrict__ w, long long n,
+__global__ void __launch_bounds__(kThr) fg_dots_kernel(const cplx<T> *__restrict__ u0, const cplx<T> *__restrict__ V,
+                                                       int nv, const cplx<T> *__restrict__ w, long long n,
                                                        double2 *__restrict__ part, const int *gate)
 {
     if (closed(gate)) return;
@@ -171,9 +174,10 @@ __global__ void __launch_bounds__(kThr) fg_dots_kernel(const cplx<T> *__restrict
 #pragma unroll
         for (int j = 0; j < MV; ++j) {
             if (j < nv) {
+                const cplx<T> *vj = j == 0 ? u0 : V + (long long)j * n;
                 cplx<T> v[kU];
 #pragma unroll
-                for (int u = 0; u < kU; ++u) v[u] = V[(long long)j * n + e + u * stride];
+                for (int u = 0; u < kU; ++u) v[u] = vj[e + u * stride];
 #pragma unroll
                 for (int u = 0; u < kU; ++u) cmac_cb(acc[j], wv[u], v[u]);  // conj(v) * w
             }
@@ -183,7 +187,7 @@ __global__ void __launch_bounds__(kThr) fg_dots_kernel(const cplx<T> *__restrict
         const cplx<T> wv = w[e];
 #pragma unroll
         for (int j = 0; j < MV; ++j)
-            if (j < nv) cmac_cb(acc[j], wv, V[(long long)j * n + e]);
+            if (j < nv) cmac_cb(acc[j], wv, (j == 0 ? u0 : V + (long long)j * n)[e]);
     }
 #pragma unroll
     for (int j = 0; j < MV; ++j) {
@@ -204,12 +208,15 @@ __device__ __forceinline__ void csub_mul(cplx<T> &a, cplx<T> v, cplx<T> h)
     a.im -= v.im * h.re;
 }
 
-// w -= sum_j V_j h_j with h summed here from the dots' partials (every CTA in the same fixed
-// order, so all agree; CTA 0 stores h in the state); per-CTA partials of ||w||^2.  nv <= MV.
+// wout = sv[k] win - sum_j V_j h_j, k = nv - 1, with h summed here from the dots' partials (every
+// CTA in the same fixed order, so all agree; CTA 0 stores h in the state) and scaled by the
+// stored vectors' factors: the basis vector j is sv[j] times stored vector j, win = A (stored
+// vector k).  Per-CTA partials of ||wout||^2.  wout may be win.  nv <= MV.
 template <typename T, int MV>
-__global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict__ V, int nv, cplx<T> *__restrict__ w,
-                                                       long long n, const double2 *__restrict__ dpart, int nparts,
-                                                       FgState *st, double *part, const int *gate)
+__global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict__ u0, const cplx<T> *__restrict__ V,
+                                                       int nv, const cplx<T> *win, cplx<T> *wout, long long n,
+                                                       const double2 *__restrict__ dpart, int nparts, FgState *st,
+                                                       double *part, const int *gate)
 {
     if (closed(gate)) return;
     __shared__ cplx<T> sh[kMaxM];
@@ -226,24 +233,31 @@ __global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict
             im += __shfl_down_sync(0xffffffffu, im, o);
         }
         if (lane == 0) {
-            sh[j] = mk<T>((T)re, (T)im);
-            if (blockIdx.x == 0) st->h[j] = mk<double>(re, im);
+            const double f = st->sv[j] * st->sv[nv - 1];
+            const cplx<double> hj = mk<double>(f * re, f * im);      // H(j+1, k+1)
+            sh[j] = mk<T>((T)(st->sv[j] * hj.re), (T)(st->sv[j] * hj.im));  // applied to stored vector j
+            if (blockIdx.x == 0) st->h[j] = hj;
         }
     }
     __syncthreads();
+    const T sk = (T)st->sv[nv - 1];
     T s = 0;
     const long long stride = (long long)gridDim.x * kThr;
     long long e = blockIdx.x * (long long)kThr + threadIdx.x;
     for (; e + (kU - 1) * stride < n; e += kU * stride) {
         cplx<T> a[kU];
 #pragma unroll
-        for (int u = 0; u < kU; ++u) a[u] = w[e + u * stride];
+        for (int u = 0; u < kU; ++u) {
+            const cplx<T> t = win[e + u * stride];
+            a[u] = mk<T>(sk * t.re, sk * t.im);
+        }
 #pragma unroll
         for (int j = 0; j < MV; ++j) {
             if (j < nv) {
+                const cplx<T> *vj = j == 0 ? u0 : V + (long long)j * n;
                 cplx<T> v[kU];
 #pragma unroll
-                for (int u = 0; u < kU; ++u) v[u] = V[(long long)j * n + e + u * stride];
+                for (int u = 0; u < kU; ++u) v[u] = vj[e + u * stride];
                 const cplx<T> hj = sh[j];
 #pragma unroll
                 for (int u = 0; u < kU; ++u) csub_mul(a[u], v[u], hj);
@@ -251,16 +265,17 @@ __global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict
         }
 #pragma unroll
         for (int u = 0; u < kU; ++u) {
-            w[e + u * stride] = a[u];
+            wout[e + u * stride] = a[u];
             s = fma(a[u].re, a[u].re, fma(a[u].im, a[u].im, s));
         }
     }
     for (; e < n; e += stride) {
-        cplx<T> a = w[e];
+        const cplx<T> t = win[e];
+        cplx<T> a = mk<T>(sk * t.re, sk * t.im);
 #pragma unroll
         for (int j = 0; j < MV; ++j)
-            if (j < nv) csub_mul(a, V[(long long)j * n + e], sh[j]);
-        w[e] = a;
+            if (j < nv) csub_mul(a, (j == 0 ? u0 : V + (long long)j * n)[e], sh[j]);
+        wout[e] = a;
         s = fma(a.re, a.re, fma(a.im, a.im, s));
     }
     const double2 t = block_sum_t<T>(s, T(0));
@@ -271,9 +286,12 @@ __global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict
 // least-squares solution of FGMRES.m:111 after the cycle's last step, is back-substituted here
 // (thread 0 of every CTA, from the rotated Hessenberg matrix) rather than after every step;
 // CTA 0 stores it in the state.
+// Stored vector 0 is u0, vector j >= 1 is B + j n; with scaled != 0 the basis vector j is sv[j]
+// times the stored one.
 template <typename T>
-__global__ void __launch_bounds__(kThr) fg_xupd_kernel(cplx<T> *__restrict__ x, const cplx<T> *__restrict__ B,
-                                                       long long n, FgState *st, const int *gate)
+__global__ void __launch_bounds__(kThr) fg_xupd_kernel(cplx<T> *__restrict__ x, const cplx<T> *__restrict__ u0,
+                                                       const cplx<T> *__restrict__ B, long long n, FgState *st,
+                                                       int scaled, const int *gate)
 {
     if (closed(gate)) return;
     __shared__ cplx<double> sR[kMaxM * kMaxM], sg[kMaxM], sy[kMaxM];
@@ -291,7 +309,8 @@ __global__ void __launch_bounds__(kThr) fg_xupd_kernel(cplx<T> *__restrict__ x, 
             sy[i] = dd == 0.0 ? mk<double>(0, 0) : (1.0 / dd) * (t * cconj(d));
         }
         for (int i = 0; i < kk; ++i) {
-            syt[i] = mk<T>((T)sy[i].re, (T)sy[i].im);
+            const double f = scaled ? st->sv[i] : 1.0;
+            syt[i] = mk<T>((T)(f * sy[i].re), (T)(f * sy[i].im));
             if (blockIdx.x == 0) st->y[i] = sy[i];
         }
     }
@@ -303,9 +322,10 @@ __global__ void __launch_bounds__(kThr) fg_xupd_kernel(cplx<T> *__restrict__ x, 
 #pragma unroll
         for (int u = 0; u < kU; ++u) a[u] = mk<T>(0, 0);
         for (int j = 0; j < kk; ++j) {
+            const cplx<T> *bj = j == 0 ? u0 : B + (long long)j * n;
             cplx<T> v[kU];
 #pragma unroll
-            for (int u = 0; u < kU; ++u) v[u] = B[(long long)j * n + e + u * stride];
+            for (int u = 0; u < kU; ++u) v[u] = bj[e + u * stride];
             const cplx<T> yj = syt[j];
 #pragma unroll
             for (int u = 0; u < kU; ++u) cmac(a[u], v[u], yj);
@@ -315,7 +335,7 @@ __global__ void __launch_bounds__(kThr) fg_xupd_kernel(cplx<T> *__restrict__ x, 
     }
     for (; e < n; e += stride) {
         cplx<T> a = mk<T>(0, 0);
-        for (int j = 0; j < kk; ++j) cmac(a, B[(long long)j * n + e], syt[j]);
+        for (int j = 0; j < kk; ++j) cmac(a, (j == 0 ? u0 : B + (long long)j * n)[e], syt[j]);
         x[e] = x[e] + a;
     }
 }
@@ -347,8 +367,9 @@ __device__ __forceinline__ bool cycles_left(int it, int m, long long maxit)
 // END OF CYCLE (first = 0, runs while live): the true residual's norm decides the break of
 // FGMRES.m:125, then the loop condition of FGMRES.m:88.  Either way the next cycle starts
 // from beta = ||r|| (FGMRES.m:92).
+// lazy: the cycle keeps its basis unnormalised (vector 0 = r itself, scale 1 / beta).
 __global__ void __launch_bounds__(kThr) fg_norm_kernel(FgState *st, const double *part, int nparts, int first,
-                                                       double tol, int m, long long maxit)
+                                                       double tol, int m, long long maxit, int lazy)
 {
     if (!first && st->hd.live == 0) return;
     const double nr = sqrt(sum_parts(part, nparts));
@@ -375,6 +396,7 @@ __global__ void __launch_bounds__(kThr) fg_norm_kernel(FgState *st, const double
     h.beta = nr;
     st->rbeta = nr != 0.0 ? 1.0 / nr : 0.0;
     st->gres = nr;
+    st->sv[0] = lazy ? st->rbeta : 1.0;
     if (first) st->rnormr0 = nr != 0.0 ? 1.0 / nr : 0.0;
     h.k = 0;
     h.go = h.live;
@@ -389,8 +411,9 @@ __global__ void __launch_bounds__(kThr) fg_norm_kernel(FgState *st, const double
 // ||w||^2), and the quasi-residual |g(j+2)| = |s| |g(j+1)| follows without a square root.
 // The state the step reads is copied to shared memory by all threads at once.
 // hist (optional): the quasi-residual history, hist[nhst] written after each step.
+// lazy: the next basis vector is kept as w itself with scale 1 / ||w||.
 __global__ void __launch_bounds__(kThr) fg_step_kernel(FgState *st, const double *part, int nparts, int j, int m,
-                                                       double tol, double *hist, const int *gate)
+                                                       double tol, double *hist, int lazy, const int *gate)
 {
     if (closed(gate)) return;
     __shared__ cplx<double> ssn[kMaxM], sc[kMaxM + 1];
@@ -451,6 +474,7 @@ __global__ void __launch_bounds__(kThr) fg_step_kernel(FgState *st, const double
     h.hst = q;
     st->hn = hn;
     st->rhn = rhn;
+    if (j + 1 < kMaxM) st->sv[j + 1] = lazy ? rhn : 1.0;
     const int nh = h.nhst + 1;
     h.nhst = nh;
     if (hist) hist[nh] = q;
@@ -572,17 +596,21 @@ int fgmres(Run &R, Fg<T> &I, const Op<T> &op, const cplx<T> *b, cplx<T> *x, bool
         ++R.launches;
         H3D_ML_LAUNCH((fg_sub_kernel<T><<<nb, kThr, 0, R.s>>>(b, I.w, I.r, n, I.part, nullptr)));
     }
-    H3D_ML_LAUNCH((fg_norm_kernel<<<1, kThr, 0, R.s>>>(I.st, I.part, I.nparts, 1, tol, m, maxit)));
+    // Unpreconditioned instances keep their basis unnormalised (each stored vector with its scale
+    // in the state): no separate scaling pass per step; vector 0 is the residual buffer itself.
+    const int lazy = pre ? 0 : 1;
+    H3D_ML_LAUNCH((fg_norm_kernel<<<1, kThr, 0, R.s>>>(I.st, I.part, I.nparts, 1, tol, m, maxit, lazy)));
     int *live = &I.st->hd.live, *go = &I.st->hd.go;
+    const cplx<T> *u0 = lazy ? I.r : I.V;
     cplx<T> *basis = pre ? I.Z : I.V;
     for (long long c = 0; c < maxit; ++c) {
         if (pre || c > 0) {
             if ((rc = R.fetch(I.st))) return rc;
             if (!R.hh->live) break;
         }
-        H3D_ML_LAUNCH((fg_scale_kernel<T><<<nb, kThr, 0, R.s>>>(I.r, I.V, n, &I.st->rbeta, live)));
+        if (!lazy) H3D_ML_LAUNCH((fg_scale_kernel<T><<<nb, kThr, 0, R.s>>>(I.r, I.V, n, &I.st->rbeta, live)));
         for (int j = 0; j < m; ++j) {
-            const cplx<T> *vj = I.V + (long long)j * n;
+            const cplx<T> *vj = j == 0 ? u0 : I.V + (long long)j * n;
             if (pre) {
                 if (j > 0) {
                     if ((rc = R.fetch(I.st))) return rc;
@@ -594,29 +622,33 @@ int fgmres(Run &R, Fg<T> &I, const Op<T> &op, const cplx<T> *b, cplx<T> *x, bool
             }
             if ((rc = launch_mvp<T>(op, vj, I.w, 1, R.adj, false, R.s))) return rc;
             ++R.launches;
+            // the orthogonalised vector: straight into the next basis slot (lazy), else into w
+            cplx<T> *wout = (lazy && j + 1 < m) ? I.V + (long long)(j + 1) * n : I.w;
             if (j < 4) {
-                H3D_ML_LAUNCH((fg_dots_kernel<T, 4><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, go)));
-                H3D_ML_LAUNCH((fg_orth_kernel<T, 4><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, I.nparts,
-                                                                          I.st, I.part, go)));
+                H3D_ML_LAUNCH((fg_dots_kernel<T, 4><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, n, I.dpart, go)));
+                H3D_ML_LAUNCH((fg_orth_kernel<T, 4><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, wout, n, I.dpart,
+                                                                          I.nparts, I.st, I.part, go)));
             } else if (j < 8) {
-                H3D_ML_LAUNCH((fg_dots_kernel<T, 8><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, go)));
-                H3D_ML_LAUNCH((fg_orth_kernel<T, 8><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, I.nparts,
-                                                                          I.st, I.part, go)));
+                H3D_ML_LAUNCH((fg_dots_kernel<T, 8><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, n, I.dpart, go)));
+                H3D_ML_LAUNCH((fg_orth_kernel<T, 8><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, wout, n, I.dpart,
+                                                                          I.nparts, I.st, I.part, go)));
             } else {
-                H3D_ML_LAUNCH((fg_dots_kernel<T, kMaxM><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart, go)));
-                H3D_ML_LAUNCH((fg_orth_kernel<T, kMaxM><<<nb, kThr, 0, R.s>>>(I.V, j + 1, I.w, n, I.dpart,
+                H3D_ML_LAUNCH((fg_dots_kernel<T, kMaxM><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, n, I.dpart, go)));
+                H3D_ML_LAUNCH((fg_orth_kernel<T, kMaxM><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, wout, n, I.dpart,
                                                                               I.nparts, I.st, I.part, go)));
             }
-            H3D_ML_LAUNCH((fg_step_kernel<<<1, kThr, 0, R.s>>>(I.st, I.part, I.nparts, j, m, tol, I.hist, go)));
-            if (j + 1 < m)
+            H3D_ML_LAUNCH(
+                (fg_step_kernel<<<1, kThr, 0, R.s>>>(I.st, I.part, I.nparts, j, m, tol, I.hist, lazy, go)));
+            if (!lazy && j + 1 < m)
                 H3D_ML_LAUNCH((fg_scale_kernel<T><<<nb, kThr, 0, R.s>>>(I.w, I.V + (long long)(j + 1) * n, n,
                                                                         &I.st->rhn, go)));
         }
-        H3D_ML_LAUNCH((fg_xupd_kernel<T><<<nb, kThr, 0, R.s>>>(x, basis, n, I.st, live)));
+        H3D_ML_LAUNCH(
+            (fg_xupd_kernel<T><<<nb, kThr, 0, R.s>>>(x, pre ? I.Z : u0, basis, n, I.st, lazy, live)));
         if ((rc = launch_mvp<T>(op, x, I.w, 1, R.adj, false, R.s))) return rc;
         ++R.launches;
         H3D_ML_LAUNCH((fg_sub_kernel<T><<<nb, kThr, 0, R.s>>>(b, I.w, I.r, n, I.part, live)));
-        H3D_ML_LAUNCH((fg_norm_kernel<<<1, kThr, 0, R.s>>>(I.st, I.part, I.nparts, 0, tol, m, maxit)));
+        H3D_ML_LAUNCH((fg_norm_kernel<<<1, kThr, 0, R.s>>>(I.st, I.part, I.nparts, 0, tol, m, maxit, lazy)));
     }
     if (last_fetch) return R.fetch(I.st);
     return H3D_OK;
