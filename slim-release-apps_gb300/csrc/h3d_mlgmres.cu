@@ -16,13 +16,15 @@
 // GB300 layout of the work.  Every vector of every level stays on the device.  Each FGMRES
 // instance (the outer solve, the smoother and coarse solver of every level, the last level's
 // inner solver) owns its Krylov basis, a partial-sum buffer and a small state block
-// (FgState) in device memory.  An Arnoldi step is five launches: the matvec, the k inner
-// products V^H w (per-CTA partial sums), the orthogonalisation w -= V h fused with the final
-// sum of those partials and with ||w||^2 partials, one single-thread step that applies the
-// previous Givens rotations to the new Hessenberg column, forms the next rotation and updates
-// the rotated right-hand side and the quasi-residual, and the scaling V(:,k+1) = w / ||w||.
-// The Givens update gives the least-squares residual norm of FGMRES.m:111-113 without a host
-// round trip; the solution y is back-substituted once per cycle, in the update of x.  Every kernel after the matvec reads
+// (FgState) in device memory.  An Arnoldi step is three launches: the matvec, the k inner
+// products V^H w (per-CTA partial sums), and the orthogonalisation w -= V h fused with the final
+// sum of those partials and with ||w||^2 partials, whose last CTA applies the previous Givens
+// rotations to the new Hessenberg column, forms the next rotation and updates the rotated
+// right-hand side and the quasi-residual.  The basis is kept unnormalised with a scale per
+// vector in the unpreconditioned instances; the preconditioned ones (whose basis vectors feed
+// the V-cycle) add a fourth launch, the scaling V(:,k+1) = w / ||w||.  The Givens update gives
+// the least-squares residual norm of FGMRES.m:111-113 without a host round trip; the solution y
+// is back-substituted once per cycle, in the update of x.  Every kernel after the matvec reads
 // a flag of the state block (the step runs / the cycle runs) and returns at once when it is
 // clear, so the host enqueues a whole unpreconditioned cycle without waiting: it
 // synchronises once per cycle there, and before each step of a preconditioned instance (to
@@ -61,6 +63,7 @@ struct FgState {
     double rhn, rbeta;          // 1 / hn and 1 / beta (0 when the norm is 0)
     double rnormr0;             // 1 / normr0
     double sv[kMaxM];           // basis vector j = sv[j] x stored vector j (1 when stored normalised)
+    int ticket;                 // CTAs of the current orthogonalisation launch that have finished
     double gres;                // |g(k+1)|: the current quasi-residual norm (before / normr0)
     double cs[kMaxM];           // Givens rotations: cosines (real) ...
     cplx<double> sn[kMaxM];     // ... and sines
@@ -198,6 +201,98 @@ __global__ void __launch_bounds__(kThr) fg_dots_kernel(const cplx<T> *__restrict
     }
 }
 
+// Sum of per-CTA partials written by other CTAs of the same launch (read through L2).
+__device__ double sum_parts_cg(const double *part, int nparts)
+{
+    double s = 0.0;
+    for (int p = threadIdx.x; p < nparts; p += kThr) s += __ldcg(part + p);
+    return block_sum_t<double>(s, 0.0).x;
+}
+
+// Step j of the cycle (0-based): H(1:j+1, j+1) = h, H(j+2, j+1) = ||w||; Givens rotations
+// replace the least-squares solve of FGMRES.m:111 (same solution and residual norm; y itself
+// is back-substituted once per cycle, by fg_xupd_kernel).  With H(j+2, j+1) = ||w|| real the
+// new rotation needs only reciprocal square roots (FP64 divisions and square roots are long
+// dependent sequences on this GPU): c = |a| / r, s = (a / |a|) ||w|| / r, r = sqrt(|a|^2 +
+// ||w||^2), and the quasi-residual |g(j+2)| = |s| |g(j+1)| follows without a square root.
+// Run by every thread of the CTA that finishes the orthogonalisation last (fg_orth_kernel); the
+// state it reads is copied to shared memory by all its threads at once.
+// hist (optional): the quasi-residual history, hist[nhst] written after each step.
+// lazy: the next basis vector is kept as w itself with scale 1 / ||w||.
+__device__ void givens_step(FgState *st, const double *part, int nparts, int j, int m, double tol, double *hist,
+                            int lazy)
+{
+    __shared__ cplx<double> ssn[kMaxM], sc[kMaxM + 1];
+    __shared__ double scs[kMaxM];
+    if (threadIdx.x < j) {
+        scs[threadIdx.x] = st->cs[threadIdx.x];
+        ssn[threadIdx.x] = st->sn[threadIdx.x];
+    }
+    if (threadIdx.x <= j) {
+        // written by CTA 0 of the same launch: read through L2
+        const double2 v = __ldcg(reinterpret_cast<const double2 *>(st->h + threadIdx.x));
+        sc[threadIdx.x] = mk<double>(v.x, v.y);
+    }
+    const double w2 = sum_parts_cg(part, nparts);  // ||w||^2 (synchronises the block)
+    if (threadIdx.x != 0) return;
+    const cplx<double> gj = st->g[j];
+    const double gres = st->gres;
+    FgHead &h = st->hd;
+    const double rnormr0 = st->rnormr0;
+    const double rhn = w2 > 0.0 ? rsqrt(w2) : 0.0;
+    const double hn = w2 * rhn;
+    cplx<double> *c = sc;
+    // rotations 0..j-1 on the column (c[i + 1] is the unrotated h[i + 1] for i + 1 <= j)
+    for (int i = 0; i < j; ++i) {
+        const double ci = scs[i];
+        const cplx<double> si = ssn[i];
+        const cplx<double> t = ci * c[i] + si * c[i + 1];
+        c[i + 1] = ci * c[i + 1] - cconj(si) * c[i];
+        c[i] = t;
+    }
+    const cplx<double> a = c[j];
+    const double na2 = cabs2(a);
+    double cj, sabs;
+    cplx<double> sj, rjj;
+    if (w2 == 0.0) {
+        cj = 1.0;
+        sj = mk<double>(0, 0);
+        sabs = 0.0;
+        rjj = a;
+    } else if (na2 == 0.0) {
+        cj = 0.0;
+        sj = mk<double>(1.0, 0.0);
+        sabs = 1.0;
+        rjj = mk<double>(hn, 0.0);
+    } else {
+        const double r2 = na2 + w2, rr = rsqrt(r2), rna = rsqrt(na2);
+        const cplx<double> ph = rna * a;
+        cj = na2 * rna * rr;
+        sabs = hn * rr;
+        sj = sabs * ph;
+        rjj = (r2 * rr) * ph;
+    }
+    c[j] = rjj;
+    st->cs[j] = cj;
+    st->sn[j] = sj;
+    for (int i = 0; i <= j; ++i) st->R[j * kMaxM + i] = c[i];
+    st->g[j + 1] = mk<double>(0, 0) - cconj(sj) * gj;
+    st->g[j] = cj * gj;
+    const double gnew = sabs * gres;
+    st->gres = gnew;
+    const double q = gnew * rnormr0;
+    h.hst = q;
+    st->hn = hn;
+    st->rhn = rhn;
+    if (j + 1 < kMaxM) st->sv[j + 1] = lazy ? rhn : 1.0;
+    const int nh = h.nhst + 1;
+    h.nhst = nh;
+    if (hist) hist[nh] = q;
+    h.it += 1;
+    h.k = j + 1;
+    h.go = (q > tol && j + 1 < m) ? 1 : 0;
+}
+
 // a -= v * h
 template <typename T>
 __device__ __forceinline__ void csub_mul(cplx<T> &a, cplx<T> v, cplx<T> h)
@@ -212,11 +307,15 @@ __device__ __forceinline__ void csub_mul(cplx<T> &a, cplx<T> v, cplx<T> h)
 // CTA in the same fixed order, so all agree; CTA 0 stores h in the state) and scaled by the
 // stored vectors' factors: the basis vector j is sv[j] times stored vector j, win = A (stored
 // vector k).  Per-CTA partials of ||wout||^2.  wout may be win.  nv <= MV.
+// The CTA that finishes last (a ticket counter in the state: every CTA publishes its partial,
+// fences, then takes a ticket; no CTA waits for another) runs the step's Givens update
+// (givens_step) for step j = nv - 1 and resets the counter.
 template <typename T, int MV>
 __global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict__ u0, const cplx<T> *__restrict__ V,
                                                        int nv, const cplx<T> *win, cplx<T> *wout, long long n,
                                                        const double2 *__restrict__ dpart, int nparts, FgState *st,
-                                                       double *part, const int *gate)
+                                                       double *part, int m, double tol, double *hist, int lazy,
+                                                       const int *gate)
 {
     if (closed(gate)) return;
     __shared__ cplx<T> sh[kMaxM];
@@ -279,7 +378,17 @@ __global__ void __launch_bounds__(kThr) fg_orth_kernel(const cplx<T> *__restrict
         s = fma(a.re, a.re, fma(a.im, a.im, s));
     }
     const double2 t = block_sum_t<T>(s, T(0));
-    if (threadIdx.x == 0) part[blockIdx.x] = t.x;
+    __shared__ int last;
+    if (threadIdx.x == 0) {
+        part[blockIdx.x] = t.x;
+        __threadfence();
+        last = atomicAdd(&st->ticket, 1) == (int)gridDim.x - 1;
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    givens_step(st, part, gridDim.x, nv - 1, m, tol, hist, lazy);
+    if (threadIdx.x == 0) st->ticket = 0;
 }
 
 // x += sum_{j < k} B_j y_j over the steps of the cycle (FGMRES.m:117-121).  y = R \ g, the
@@ -397,90 +506,13 @@ __global__ void __launch_bounds__(kThr) fg_norm_kernel(FgState *st, const double
     st->rbeta = nr != 0.0 ? 1.0 / nr : 0.0;
     st->gres = nr;
     st->sv[0] = lazy ? st->rbeta : 1.0;
-    if (first) st->rnormr0 = nr != 0.0 ? 1.0 / nr : 0.0;
+    if (first) {
+        st->rnormr0 = nr != 0.0 ? 1.0 / nr : 0.0;
+        st->ticket = 0;
+    }
     h.k = 0;
     h.go = h.live;
     st->g[0] = mk<double>(nr, 0.0);
-}
-
-// Step j of the cycle (0-based): H(1:j+1, j+1) = h, H(j+2, j+1) = ||w||; Givens rotations
-// replace the least-squares solve of FGMRES.m:111 (same solution and residual norm; y itself
-// is back-substituted once per cycle, by fg_xupd_kernel).  With H(j+2, j+1) = ||w|| real the
-// new rotation needs only reciprocal square roots (FP64 divisions and square roots are long
-// dependent sequences on this GPU): c = |a| / r, s = (a / |a|) ||w|| / r, r = sqrt(|a|^2 +
-// ||w||^2), and the quasi-residual |g(j+2)| = |s| |g(j+1)| follows without a square root.
-// The state the step reads is copied to shared memory by all threads at once.
-// hist (optional): the quasi-residual history, hist[nhst] written after each step.
-// lazy: the next basis vector is kept as w itself with scale 1 / ||w||.
-__global__ void __launch_bounds__(kThr) fg_step_kernel(FgState *st, const double *part, int nparts, int j, int m,
-                                                       double tol, double *hist, int lazy, const int *gate)
-{
-    if (closed(gate)) return;
-    __shared__ cplx<double> ssn[kMaxM], sc[kMaxM + 1];
-    __shared__ double scs[kMaxM];
-    if (threadIdx.x < j) {
-        scs[threadIdx.x] = st->cs[threadIdx.x];
-        ssn[threadIdx.x] = st->sn[threadIdx.x];
-    }
-    if (threadIdx.x <= j) sc[threadIdx.x] = st->h[threadIdx.x];
-    const double w2 = sum_parts(part, nparts);  // ||w||^2 (synchronises the block)
-    if (threadIdx.x != 0) return;
-    const cplx<double> gj = st->g[j];
-    const double gres = st->gres;
-    FgHead &h = st->hd;
-    const double rnormr0 = st->rnormr0;
-    const double rhn = w2 > 0.0 ? rsqrt(w2) : 0.0;
-    const double hn = w2 * rhn;
-    cplx<double> *c = sc;
-    // rotations 0..j-1 on the column (c[i + 1] is the unrotated h[i + 1] for i + 1 <= j)
-    for (int i = 0; i < j; ++i) {
-        const double ci = scs[i];
-        const cplx<double> si = ssn[i];
-        const cplx<double> t = ci * c[i] + si * c[i + 1];
-        c[i + 1] = ci * c[i + 1] - cconj(si) * c[i];
-        c[i] = t;
-    }
-    const cplx<double> a = c[j];
-    const double na2 = cabs2(a);
-    double cj, sabs;
-    cplx<double> sj, rjj;
-    if (w2 == 0.0) {
-        cj = 1.0;
-        sj = mk<double>(0, 0);
-        sabs = 0.0;
-        rjj = a;
-    } else if (na2 == 0.0) {
-        cj = 0.0;
-        sj = mk<double>(1.0, 0.0);
-        sabs = 1.0;
-        rjj = mk<double>(hn, 0.0);
-    } else {
-        const double r2 = na2 + w2, rr = rsqrt(r2), rna = rsqrt(na2);
-        const cplx<double> ph = rna * a;
-        cj = na2 * rna * rr;
-        sabs = hn * rr;
-        sj = sabs * ph;
-        rjj = (r2 * rr) * ph;
-    }
-    c[j] = rjj;
-    st->cs[j] = cj;
-    st->sn[j] = sj;
-    for (int i = 0; i <= j; ++i) st->R[j * kMaxM + i] = c[i];
-    st->g[j + 1] = mk<double>(0, 0) - cconj(sj) * gj;
-    st->g[j] = cj * gj;
-    const double gnew = sabs * gres;
-    st->gres = gnew;
-    const double q = gnew * rnormr0;
-    h.hst = q;
-    st->hn = hn;
-    st->rhn = rhn;
-    if (j + 1 < kMaxM) st->sv[j + 1] = lazy ? rhn : 1.0;
-    const int nh = h.nhst + 1;
-    h.nhst = nh;
-    if (hist) hist[nh] = q;
-    h.it += 1;
-    h.k = j + 1;
-    h.go = (q > tol && j + 1 < m) ? 1 : 0;
 }
 
 // ---- host side -------------------------------------------------------------------------------
@@ -627,18 +659,19 @@ int fgmres(Run &R, Fg<T> &I, const Op<T> &op, const cplx<T> *b, cplx<T> *x, bool
             if (j < 4) {
                 H3D_ML_LAUNCH((fg_dots_kernel<T, 4><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, n, I.dpart, go)));
                 H3D_ML_LAUNCH((fg_orth_kernel<T, 4><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, wout, n, I.dpart,
-                                                                          I.nparts, I.st, I.part, go)));
+                                                                          I.nparts, I.st, I.part, m, tol, I.hist,
+                                                                          lazy, go)));
             } else if (j < 8) {
                 H3D_ML_LAUNCH((fg_dots_kernel<T, 8><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, n, I.dpart, go)));
                 H3D_ML_LAUNCH((fg_orth_kernel<T, 8><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, wout, n, I.dpart,
-                                                                          I.nparts, I.st, I.part, go)));
+                                                                          I.nparts, I.st, I.part, m, tol, I.hist,
+                                                                          lazy, go)));
             } else {
                 H3D_ML_LAUNCH((fg_dots_kernel<T, kMaxM><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, n, I.dpart, go)));
                 H3D_ML_LAUNCH((fg_orth_kernel<T, kMaxM><<<nb, kThr, 0, R.s>>>(u0, I.V, j + 1, I.w, wout, n, I.dpart,
-                                                                              I.nparts, I.st, I.part, go)));
+                                                                              I.nparts, I.st, I.part, m, tol, I.hist,
+                                                                          lazy, go)));
             }
-            H3D_ML_LAUNCH(
-                (fg_step_kernel<<<1, kThr, 0, R.s>>>(I.st, I.part, I.nparts, j, m, tol, I.hist, lazy, go)));
             if (!lazy && j + 1 < m)
                 H3D_ML_LAUNCH((fg_scale_kernel<T><<<nb, kThr, 0, R.s>>>(I.w, I.V + (long long)(j + 1) * n, n,
                                                                         &I.st->rhn, go)));
