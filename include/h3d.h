@@ -39,7 +39,9 @@
  *                      (construct_multigrid.m:45-51, fine2coarse.m:40-55: Kronecker
  *                       products of 1D interpolation operators, one axis per call)
  *   h3d_mlgmres_solve  linearsolve with SOLVE_FGMRES and PREC_MLGMRES (FGMRES.m, ML_GMRES.m,
- *                      opMultigrid.m): the 3D applications' default solver
+ *                      opMultigrid.m): the 3D applications' default solver; _model and the
+ *                      h3d_mex_mlgmres host entry build the hierarchy from the physical model
+ *                      (construct_multigrid.m)
  *   h3d_band_coefs     the band-storage (mat_free = false) operator: helmholtz_3d.m:35-190
  *                      (27 x N bands of H) and conj(Htransp(H)) (opBandStorage.m:127-129)
  *   h3d_band_mvp       Hmvp_MT_mex (Hmvp_MT_mex.c:53-73, via Hmvp.m / opBandStorage.multiply)
@@ -369,6 +371,9 @@ typedef struct h3d_ml_info {
 
 void h3d_ml_default_opts(h3d_ml_opts *opts);
 
+/* Units of a velocity model (param2wavenum.m): m/s, s^2/m^2, s^2/km^2. */
+typedef enum { H3D_UNIT_M_PER_S = 0, H3D_UNIT_S2_PER_M2 = 1, H3D_UNIT_S2_PER_KM2 = 2 } h3d_unit;
+
 /* x = H \ b (mode FORWARD) or H^H \ b (ADJOINT) by FGMRES (FGMRES.m:33-129) preconditioned by
  * the recursive ML_GMRES V-cycle over `nlevels` levels (ML_GMRES.m:36-72, opMultigrid.m;
  * linearsolve.m:139-141 with discrete_helmholtz.m:349-350), or by nothing (PREC_NONE: plain
@@ -383,6 +388,39 @@ int h3d_mlgmres_solve(const h3d_ml_level *levels, int nlevels, const h3d_ml_tran
                       const h3d_ml_transfer *prolong_ops, const void *b, void *x, int mode,
                       const h3d_ml_opts *opts, double *hst, int hst_cap, h3d_ml_info *info,
                       void *stream);
+
+/* The same solve from the physical model: the hierarchy of construct_multigrid.m:10-60 built by
+ * the library (level i: the model coarsened i times by opLInterp1D's 4-point Lagrange
+ * interpolation to ceil(n/2) points per axis, spacing 2^i h, ceil(npml/2^i) PML points with the
+ * model edge-replicated into them, param2wavenum; transfers: LinInterp1D between the
+ * computational grids, restriction = prolongation^T / 8), then h3d_mlgmres_solve.  v_phys:
+ * host, n_phys[0] x n_phys[1] x n_phys[2], x fastest, in `unit` (h3d_unit); every axis of a
+ * level that is coarsened needs 4 or more points.  b, x: device, complex128, on the level-0
+ * PML grid (n_phys + 2 npml per axis).  Synchronises `stream`. */
+int h3d_mlgmres_solve_model(const double *v_phys, const int32_t n_phys[3], const double h[3], int npml,
+                            double freq, int unit, int nlevels, const void *b, void *x, int mode,
+                            const h3d_ml_opts *opts, double *hst, int hst_cap, h3d_ml_info *info,
+                            void *stream);
+
+/* Host entry of the h3d_mlgmres_mex gateway: MATLAB's split-complex host arrays (b, u:
+ * b_rows x nrhs, column-major; b_im may be NULL), n_phys as three doubles, npml a
+ * non-negative integer.  Each column is an independent FGMRES solve from zero (the
+ * hierarchy is built once).  b_rows != prod(n_phys + 2 npml) gives H3D_ERR_BSIZE, a bad n
+ * H3D_ERR_NSIZE.  info: iters / rel_res the maximum over columns, converged all of them,
+ * seconds / launches / waits summed.  Synchronous. */
+int h3d_mex_mlgmres(const double *v_phys, const double *n_phys, size_t n_len, const double *h,
+                    double npml, double freq, int unit, int nlevels, const double *b_re,
+                    const double *b_im, size_t b_rows, size_t nrhs, double *u_re, double *u_im,
+                    int mode, const h3d_ml_opts *opts, h3d_ml_info *info);
+
+/* Host-only pieces of the hierarchy (no device call), exported for callers that build their
+ * own levels and for tests: dense nout x nin row-major interpolation weights from the
+ * ascending nodes xin to the ascending points xout, kind 0 = linear (LinInterp1D.m via
+ * nearestnbr1d.m), 1 = 4-point Lagrange (opLInterp1D.m getLA; nin >= 4; points outside the
+ * nodes give zero rows); and the model coarsening (x fastest; every axis of n >= 4 points)
+ * as the separable product of the Lagrange weights on linspace(0, 1, n) nodes. */
+int h3d_ml_interp_weights(int kind, const double *xin, int nin, const double *xout, int nout, double *A);
+int h3d_ml_coarsen_model(const double *v, const int32_t n[3], const int32_t n_sub[3], double *v_sub);
 
 /* ---- band storage (the reference's mat_free = false path) ---------------------------- */
 /* A band matrix holds ndiags couplings per row: coef[k + ndiags*i] = A(i, i + offsets[k])

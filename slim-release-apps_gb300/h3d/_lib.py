@@ -87,6 +87,8 @@ class MLInfo(C.Structure):
 
 
 ML_PREC_NONE, ML_PREC_MLGMRES = 0, 1
+UNIT_M_PER_S, UNIT_S2_PER_M2, UNIT_S2_PER_KM2 = 0, 1, 2
+UNITS = {"m/s": UNIT_M_PER_S, "s2/m2": UNIT_S2_PER_M2, "s2/km2": UNIT_S2_PER_KM2}
 
 
 class H3DError(RuntimeError):
@@ -137,6 +139,12 @@ _SIGS = {
     "h3d_axis_apply": (C.c_int, [vp, vp, vp, C.c_int, C.c_int, C.POINTER(C.c_int32), vp, vp, C.c_int,
                                  C.c_int, vp]),
     "h3d_ml_default_opts": (None, [C.POINTER(MLOpts)]),
+    "h3d_ml_interp_weights": (C.c_int, [C.c_int, dp, C.c_int, dp, C.c_int, dp]),
+    "h3d_ml_coarsen_model": (C.c_int, [dp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp]),
+    "h3d_mlgmres_solve_model": (C.c_int, [dp, C.POINTER(C.c_int32), dp, C.c_int, C.c_double, C.c_int, C.c_int, vp,
+                                          vp, C.c_int, C.POINTER(MLOpts), dp, C.c_int, C.POINTER(MLInfo), vp]),
+    "h3d_mex_mlgmres": (C.c_int, [dp, dp, C.c_size_t, dp, C.c_double, C.c_double, C.c_int, C.c_int, dp, dp,
+                                  C.c_size_t, C.c_size_t, dp, dp, C.c_int, C.POINTER(MLOpts), C.POINTER(MLInfo)]),
     "h3d_mlgmres_solve": (C.c_int, [C.POINTER(MLLevel), C.c_int, C.POINTER(MLTransfer), C.POINTER(MLTransfer),
                                     vp, vp, C.c_int, C.POINTER(MLOpts), dp, C.c_int, C.POINTER(MLInfo), vp]),
     "h3d_band_coefs": (C.c_int, [C.POINTER(Grid), vp, vp, C.c_int, vp, C.POINTER(C.c_int64), C.c_int, vp]),

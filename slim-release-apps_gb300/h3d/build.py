@@ -49,6 +49,8 @@ MEX_VARIANTS = {
     "sweep_MT_mex": ("bswp", []),
     # the whole linearsolve / CGMN solve in one call (no reference binary of this name)
     "h3d_solve_mex": ("solve", []),
+    # FGMRES + ML_GMRES from the physical model in one call (no reference binary of this name)
+    "h3d_mlgmres_mex": ("mlgmres", []),
 }
 
 
@@ -151,7 +153,8 @@ def build_mex(verbose: bool = False, force: bool = False) -> dict:
         if not force and _newer(so, [gw, stub_c, LIB, os.path.join(INCLUDE, "h3d.h")]):
             continue
         kflag = {"mvp": "-DH3D_GATEWAY_MVP", "swp": "-DH3D_GATEWAY_SWEEP", "bmvp": "-DH3D_GATEWAY_BAND_MVP",
-                 "bswp": "-DH3D_GATEWAY_BAND_SWEEP", "solve": "-DH3D_GATEWAY_SOLVE"}[kind]
+                 "bswp": "-DH3D_GATEWAY_BAND_SWEEP", "solve": "-DH3D_GATEWAY_SOLVE",
+                 "mlgmres": "-DH3D_GATEWAY_MLGMRES"}[kind]
         tmp = f"{so}.{os.getpid()}.tmp"
         _run([cc, "-O2", "-std=c11", "-fPIC", "-shared", kflag, *flags, "-I", INCLUDE, "-I",
               stub_dir, gw, stub_c, "-o", tmp, "-L", LIBDIR, "-lh3d",

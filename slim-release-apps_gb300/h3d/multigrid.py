@@ -17,8 +17,10 @@ after 5 steps) preconditioned by ML_GMRES (fwi_exp.m:58-62, discrete_helmholtz.m
 
 The solve itself is one library call (h3d_mlgmres_solve): the FGMRES control flow in C++,
 every Arnoldi step, Givens rotation and stopping test on the device, the library's 27-point
-matvec and its axis kernel for the grid transfers.  Model coarsening and interpolation
-weights are set-up work on the host (this module).
+matvec and its axis kernel for the grid transfers.  The interpolation weights and the model
+coarsening are the library's host code (h3d_ml_interp_weights, h3d_ml_coarsen_model); this
+module assembles the levels from them, or solve_model hands the physical model to the library
+(h3d_mlgmres_solve_model).
 """
 from __future__ import annotations
 
@@ -32,64 +34,38 @@ from . import _lib as L
 from . import ops
 
 
-# ---- interpolation weights (host) -------------------------------------------------------------
-def _nearest(xin, xout):
-    """Index of the nearest input node per output node, ties to the lower node
-    (nearestnbr1d.m); both grids ascending."""
-    idx = np.searchsorted(xin, xout, side="left")
-    lo = np.clip(idx - 1, 0, len(xin) - 1)
-    hi = np.clip(idx, 0, len(xin) - 1)
-    return np.where(np.abs(xout - xin[lo]) <= np.abs(xout - xin[hi]), lo, hi)
+# ---- interpolation weights and model coarsening (the library's host code) -----------------------
+def _weights(kind, xin, xout):
+    xin = np.ascontiguousarray(xin, float)
+    xout = np.ascontiguousarray(xout, float)
+    A = np.zeros((len(xout), len(xin)))
+    rc = L.load().h3d_ml_interp_weights(kind, xin.ctypes.data_as(L.dp), len(xin), xout.ctypes.data_as(L.dp),
+                                        len(xout), A.ctypes.data_as(L.dp))
+    L.check(rc, "h3d_ml_interp_weights")
+    return A
 
 
 def linear_weights(xin, xout):
-    """LinInterp1D.m: CSR (rowptr, col, val) of the len(xout) x len(xin) linear interpolation."""
-    xin = np.sort(np.asarray(xin, float))
-    xout = np.sort(np.asarray(xout, float))
-    nin, nout = len(xin), len(xout)
-    I = _nearest(xin, xout)
-    I = np.where(xin[I] > xout, I - 1, I)
-    nxt = np.where(I + 1 < nin, xin[np.minimum(I + 1, nin - 1)], 1e12)
-    wb = (xout - xin[I]) / (nxt - xin[I])
-    wa = (nxt - xout) / (nxt - xin[I])
-    dense = np.zeros((nout, nin))
-    np.add.at(dense, (np.arange(nout), I), wa)
-    np.add.at(dense, (np.arange(nout), np.minimum(I + 1, nin - 1)), wb)
-    return dense
+    """LinInterp1D.m: the len(xout) x len(xin) linear interpolation (dense)."""
+    return _weights(0, np.sort(np.asarray(xin, float)), np.sort(np.asarray(xout, float)))
 
 
 def cubic_weights(x1, x2):
     """opLInterp1D.m getLA: len(x2) x len(x1) 4-point Lagrange interpolation (zero rows
-    for points outside the node range); the node window slides monotonically as there."""
-    x1 = np.asarray(x1, float)
-    x2 = np.asarray(x2, float)
-    n1 = len(x1)
-    A = np.zeros((len(x2), n1))
-    b, c = 1, 2
-    for k in np.nonzero((x2 >= x1[0]) & (x2 <= x1[-1]))[0]:
-        X = x2[k]
-        if X < x1[b]:
-            while X < x1[b] and b > 1:
-                b -= 1
-            c = b + 1
-        elif X > x1[c]:
-            while X > x1[c] and c < n1 - 2:
-                c += 1
-            b = c - 1
-        nodes = (b - 1, b, c, c + 1)
-        for p in nodes:
-            others = [q for q in nodes if q != p]
-            A[k, p] += np.prod([X - x1[q] for q in others]) / np.prod([x1[p] - x1[q] for q in others])
-    return A
+    for points outside the node range)."""
+    return _weights(1, x1, x2)
 
 
 def _coarsen_model(v, n_sub):
-    """Physical model on ceil(n/2) points per axis by separable cubic interpolation."""
-    g = lambda m: np.linspace(0.0, 1.0, int(m))
-    Ax, Ay, Az = (cubic_weights(g(v.shape[a]), g(n_sub[a])) for a in range(3))
-    t = np.tensordot(Ax, v, axes=(1, 0))                        # (a, j, k)
-    t = np.tensordot(Ay, t, axes=(1, 1)).transpose(1, 0, 2)     # (a, b, k)
-    return np.tensordot(t, Az, axes=(2, 1))                     # (a, b, c)
+    """Physical model on n_sub points per axis by separable cubic interpolation."""
+    v = np.asarray(v, float)
+    n = (C.c_int32 * 3)(*v.shape)
+    ns = (C.c_int32 * 3)(*(int(x) for x in n_sub))
+    src = np.ascontiguousarray(v.reshape(-1, order="F"))
+    out = np.zeros(int(np.prod(n_sub)))
+    rc = L.load().h3d_ml_coarsen_model(src.ctypes.data_as(L.dp), n, ns, out.ctypes.data_as(L.dp))
+    L.check(rc, "h3d_ml_coarsen_model")
+    return out.reshape(tuple(int(x) for x in n_sub), order="F")
 
 
 def _extend(v, npml):
@@ -250,6 +226,42 @@ def solve(levels, R, P, b: torch.Tensor, tol=1e-6, maxit=10000, maxinnerit=5, mo
                                ops._mode(mode), C.byref(o), hst.ctypes.data_as(L.dp), int(hst.size),
                                C.byref(info), C.c_void_p(st))
     L.check(rc, "h3d_mlgmres_solve")
+    d = info.as_dict()
+    d["hst"] = hst[: info.iters + 1].tolist()
+    return u, d
+
+
+def solve_model(v_phys, dt, npml, freq, b: torch.Tensor, unit="m/s", nlevels=3, tol=1e-6, maxit=10000,
+                maxinnerit=5, mode=1, precision="fp64", k=(3, 5, 3, 5), coarse_tol=0.5):
+    """The same solve with the hierarchy built by the library from the physical model
+    (h3d_mlgmres_solve_model: construct_multigrid.m in C++, one call).  v_phys: (nx, ny, nz)
+    array; b on the level-0 PML grid."""
+    if precision not in ("fp64", "mixed"):
+        raise ValueError(f"precision must be 'fp64' or 'mixed', not {precision!r}")
+    lib = L.load()
+    v = np.asarray(v_phys, float)
+    src = np.ascontiguousarray(v.reshape(-1, order="F"))
+    n = (C.c_int32 * 3)(*v.shape)
+    h = np.ascontiguousarray(np.broadcast_to(np.asarray(dt, float), (3,)))
+    b = b.to(torch.complex128).contiguous()
+    u = torch.zeros_like(b)
+    o = L.MLOpts()
+    lib.h3d_ml_default_opts(C.byref(o))
+    o.tol = float(tol)
+    o.maxit = int(min(maxit, 2 ** 31 - 1))
+    o.maxinnerit = int(maxinnerit)
+    o.precision = L.PREC_FP64 if precision == "fp64" else L.PREC_MIXED
+    for i in range(4):
+        o.k[i] = int(k[i])
+    o.coarse_tol = float(coarse_tol)
+    hst = np.zeros(1 + o.maxit * o.maxinnerit)
+    info = L.MLInfo()
+    st = torch.cuda.current_stream(b.device).cuda_stream
+    rc = lib.h3d_mlgmres_solve_model(src.ctypes.data_as(L.dp), n, h.ctypes.data_as(L.dp), int(npml), float(freq),
+                                     L.UNITS[unit], int(nlevels), C.c_void_p(b.data_ptr()), C.c_void_p(u.data_ptr()),
+                                     ops._mode(mode), C.byref(o), hst.ctypes.data_as(L.dp), int(hst.size),
+                                     C.byref(info), C.c_void_p(st))
+    L.check(rc, "h3d_mlgmres_solve_model")
     d = info.as_dict()
     d["hst"] = hst[: info.iters + 1].tolist()
     return u, d

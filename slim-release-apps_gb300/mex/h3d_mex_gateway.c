@@ -20,6 +20,15 @@
  *       CGMN.m:79's preconditioned residual.  Returns the last iterate when maxit is reached,
  *       as CGMN.m does.
  *
+ *   -DH3D_GATEWAY_MLGMRES                              -> h3d_mlgmres_mex (no reference binary)
+ *       u = h3d_mlgmres_mex(v, h, n, npml, freq, b, mode, tol, maxit[, precision[, unit]])
+ *       linearsolve.m:139-141 with SOLVE_FGMRES preconditioned by ML_GMRES
+ *       (discrete_helmholtz.m:349-350): the three-level hierarchy of construct_multigrid.m
+ *       built from the physical model v (n = its three sizes, npml PML points added on every
+ *       face, h the spacing, unit 0 = m/s (default), 1 = s2/m2, 2 = s2/km2) and FGMRES
+ *       (restart 5) to tol on the PML grid; precision 0 = FP64 (default), 1 = complex64
+ *       V-cycle under the complex128 FGMRES.  Each column of b is solved independently.
+ *
  * Same argument order, same checks and error identifiers as the reference
  * gateways, same output (a new N x 1 or N x P complex double matrix).  The
  * arithmetic runs on the GPU through libh3d (include/h3d.h); nthreads is
@@ -186,6 +195,36 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
     if (rc != H3D_OK && rc != H3D_ERR_NOT_CONVERGED) fail(rc, "h3d_solve_mex");
 }
 
+#elif defined(H3D_GATEWAY_MLGMRES)
+
+void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
+{
+    (void)nlhs;
+    if (nrhs < 9)
+        mexErrMsgIdAndTxt("h3d:badArgument", "expected (v,h,n,npml,freq,b,mode,tol,maxit[,precision[,unit]])");
+    const mxArray *V = prhs[0], *H = prhs[1], *N = prhs[2], *B = prhs[5];
+    const size_t nl = n_len_of(N);
+    if (nl != 3) {
+        fail(H3D_ERR_NSIZE, "h3d_mlgmres_mex");
+        return;
+    }
+    const double *n = mxGetPr(N);
+    const double npml = mxGetScalar(prhs[3]);
+    h3d_ml_opts o;
+    h3d_ml_default_opts(&o);
+    o.tol = mxGetScalar(prhs[7]);
+    o.maxit = (int32_t)mxGetScalar(prhs[8]);
+    if (nrhs > 9) o.precision = mxGetScalar(prhs[9]) != 0.0 ? H3D_PREC_MIXED : H3D_PREC_FP64;
+    const int unit = nrhs > 10 ? (int)mxGetScalar(prhs[10]) : H3D_UNIT_M_PER_S;
+    const int mode = mxGetScalar(prhs[6]) == 1.0 ? H3D_FORWARD : H3D_ADJOINT;   /* linearsolve.m:52-60 */
+    const size_t P = mxGetN(B), rows = mxGetM(B);
+    plhs[0] = mxCreateDoubleMatrix(rows, P, mxCOMPLEX);
+    int rc = h3d_mex_mlgmres(mxGetPr(V), n, nl, mxGetPr(H), npml, mxGetScalar(prhs[4]), unit, 3, mxGetPr(B),
+                             mxIsComplex(B) ? mxGetPi(B) : NULL, rows, P, mxGetPr(plhs[0]), mxGetPi(plhs[0]), mode,
+                             &o, NULL);
+    if (rc != H3D_OK) fail(rc, "h3d_mlgmres_mex");
+}
+
 #elif defined(H3D_GATEWAY_BAND_MVP) || defined(H3D_GATEWAY_BAND_SWEEP)
 
 #define BAND_ID ID_PREFIX "HMvp_MT_mex:NumElements"
@@ -250,5 +289,5 @@ void mexFunction(int nlhs, mxArray *plhs[], int nrhs, const mxArray *prhs[])
 #endif
 
 #else
-#error "define H3D_GATEWAY_MVP, H3D_GATEWAY_SWEEP, H3D_GATEWAY_BAND_MVP or H3D_GATEWAY_BAND_SWEEP"
+#error "define H3D_GATEWAY_MVP, _SWEEP, _SOLVE, _MLGMRES, _BAND_MVP or _BAND_SWEEP"
 #endif

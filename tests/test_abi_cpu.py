@@ -212,3 +212,39 @@ def test_mlgmres_refuses_bad_arguments_without_a_gpu():
     hst = np.zeros(10)
     assert call(1, o4, hst.ctypes.data_as(L.dp), 10) == L.ERR_BAD_ARG   # 1 + 2 x 5 entries needed
     assert b"hst holds 10" in lib.h3d_last_error()
+
+
+def test_multigrid_host_pieces_and_gateway_refuse_bad_input_without_a_gpu():
+    """The hierarchy's host code checks its inputs (cubic weights need 4 nodes, nodes must
+    ascend), and the h3d_mlgmres_mex gateway reports a bad n and a b of the wrong height with
+    its Nsize / Bsize identifiers before any device call."""
+    from h3d import _lib as L
+    from h3d import build
+    from oracle import mexharness as M
+
+    lib = L.load()
+    x3 = np.linspace(0.0, 1.0, 3)
+    out = np.zeros(9)
+    assert lib.h3d_ml_interp_weights(1, x3.ctypes.data_as(L.dp), 3, x3.ctypes.data_as(L.dp), 3,
+                                     out.ctypes.data_as(L.dp)) == L.ERR_BAD_ARG
+    down = x3[::-1].copy()
+    assert lib.h3d_ml_interp_weights(0, down.ctypes.data_as(L.dp), 3, x3.ctypes.data_as(L.dp), 3,
+                                     out.ctypes.data_as(L.dp)) == L.ERR_BAD_ARG
+    # partition of unity of both interpolations between linspace nodes
+    xi, xo = np.linspace(0.0, 1.0, 9), np.linspace(0.0, 1.0, 5)
+    for kind in (0, 1):
+        A = np.zeros((5, 9))
+        assert lib.h3d_ml_interp_weights(kind, xi.ctypes.data_as(L.dp), 9, xo.ctypes.data_as(L.dp), 5,
+                                         A.ctypes.data_as(L.dp)) == L.OK
+        np.testing.assert_allclose(A.sum(axis=1), 1.0, atol=1e-14)
+        np.testing.assert_allclose(A @ xi, xo, atol=1e-14)           # both reproduce linear functions
+
+    gw = M.MexFunction(build.build_mex()["h3d_mlgmres_mex"])
+    v = np.full(6 * 5 * 4, 1500.0)
+    h = np.full(3, 20.0)
+    with pytest.raises(M.MexError) as e:
+        gw(v, h, np.ones((2, 2)), 2.0, 4.0, np.ones(10), 1.0, 1e-6, 10.0)
+    assert e.value.ident == "SLIM_release_apps:tools:algorithms:ThreeDFreqModeling:h3d_mlgmres_mex:Nsize"
+    with pytest.raises(M.MexError) as e:                              # b must cover the PML grid
+        gw(v, h, np.array([6.0, 5.0, 4.0]), 2.0, 4.0, np.ones(6 * 5 * 4), 1.0, 1e-6, 10.0)
+    assert e.value.ident == "SLIM_release_apps:tools:algorithms:ThreeDFreqModeling:h3d_mlgmres_mex:Bsize"

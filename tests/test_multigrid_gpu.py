@@ -129,3 +129,30 @@ def test_mixed_precision_cycle_converges(cuda):
     for u in (u64, u32):
         assert float((b - lv[0].A(u)).norm() / b.norm()) <= 1e-6
     assert i32["iters"] <= i64["iters"] + 5
+
+
+def test_hierarchy_built_by_the_library_and_mex_gateway(cuda):
+    """h3d_mlgmres_solve_model (construct_multigrid in the library's host code) and the
+    h3d_mlgmres_mex gateway (MATLAB host arrays, two columns) give the solve on the levels
+    assembled here: same outer iterations, same solution to rounding (FP64)."""
+    import torch
+    from h3d import build
+    from h3d import multigrid as MG
+    from oracle import mexharness as M
+
+    v, dt, npml, f = _model(seed=4)
+    lv, R, P = MG.build_levels(v, dt, npml, f, "m/s", device=cuda)
+    N = int(np.prod(lv[0].nt))
+    rng = np.random.default_rng(9)
+    B = rng.standard_normal((N, 2)) + 1j * rng.standard_normal((N, 2))
+    ref = [MG.solve(lv, R, P, torch.as_tensor(B[:, c].copy(), device=cuda), tol=1e-8) for c in range(2)]
+    u, info = MG.solve_model(v, dt, npml, f, torch.as_tensor(B[:, 0].copy(), device=cuda), tol=1e-8)
+    assert info["iters"] == ref[0][1]["iters"] and info["converged"] == 1
+    r0 = ref[0][0].cpu().numpy()
+    assert np.linalg.norm(u.cpu().numpy() - r0) <= 1e-10 * np.linalg.norm(r0)
+    gw = M.MexFunction(build.build_mex()["h3d_mlgmres_mex"])
+    U = gw(np.asarray(v, float).reshape(-1, order="F"), np.asarray(dt, float), np.array(v.shape, float),
+           float(npml), f, B, 1.0, 1e-8, 10000.0)
+    for c in range(2):
+        rc = ref[c][0].cpu().numpy()
+        assert np.linalg.norm(U[:, c] - rc) <= 1e-10 * np.linalg.norm(rc)
