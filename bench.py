@@ -22,7 +22,8 @@ Reported (one JSON line on rank 0):
              outer iterations, the mixed wavefield against the oracle's
   batched    the 256-right-hand-side batch (64 surface sources x 3/4/5/6 Hz, Ricker weights)
              as one batched mixed solve with its sweep's live roofline, beside plain FP64 solves
-             of a sample of it (speed-up per solve, wavefield difference on the sample)
+             of a sample of it (speed-up per solve, wavefield difference on the sample), and
+             the same right-hand sides one at a time by FGMRES + ML_GMRES (batched.mlgmres)
   fwi        the FWI gradient of the 161 x 161 x 81 workload (32 sources x 3 frequencies, 400
              receivers) in mixed precision, beside a plain-FP64 gradient of a sample of its
              (source, frequency) pairs, the same gradient with every solve by FGMRES + ML_GMRES
@@ -326,6 +327,10 @@ def run_batched(args):
         del u64
     del us
     torch.cuda.empty_cache()
+    if not args.skip_batch_mlgmres:
+        # the same 256 right-hand sides one at a time by FGMRES + ML_GMRES
+        out["mlgmres"] = W.config2_mlgmres(precision="mixed", nsrc=args.batch_nsrc)
+        torch.cuda.empty_cache()
     return out
 
 
@@ -568,6 +573,7 @@ def main():
     ap.add_argument("--skip-batched", action="store_true")
     ap.add_argument("--skip-mlgmres", action="store_true")
     ap.add_argument("--skip-fwi-mlgmres", action="store_true", help="no config-3 gradient by the multigrid solver")
+    ap.add_argument("--skip-batch-mlgmres", action="store_true", help="no config-2 solves by the multigrid solver")
     ap.add_argument("--mlgmres-reps", type=int, default=3, help="timed config-1 FGMRES + ML_GMRES solves")
     ap.add_argument("--skip-fwi", action="store_true")
     ap.add_argument("--skip-config0", action="store_true", help="reference arm: no full config-0 CPU solve")
