@@ -421,6 +421,11 @@ int h3d_mex_mlgmres(const double *v_phys, const double *n_phys, size_t n_len, co
  * as the separable product of the Lagrange weights on linspace(0, 1, n) nodes. */
 int h3d_ml_interp_weights(int kind, const double *xin, int nin, const double *xout, int nout, double *A);
 int h3d_ml_coarsen_model(const double *v, const int32_t n[3], const int32_t n_sub[3], double *v_sub);
+/* The levels h3d_mlgmres_solve_model builds, on the host: grids[i] (n with PML, spacing, PML
+ * widths) and the FP64 wavenumbers of levels 0..nlevels-1 one after the other in wn (wn_cap
+ * values; too small gives H3D_ERR_BAD_ARG with the size needed in the message). */
+int h3d_ml_levels_host(const double *v_phys, const int32_t n_phys[3], const double h[3], int npml, double freq,
+                       int unit, int nlevels, h3d_grid *grids, double *wn, size_t wn_cap);
 
 /* ---- band storage (the reference's mat_free = false path) ---------------------------- */
 /* A band matrix holds ndiags couplings per row: coef[k + ndiags*i] = A(i, i + offsets[k])

@@ -203,8 +203,9 @@ struct MlPlan {
     DevBuf dev;
 };
 
-int ml_plan_build(const double *v_phys, const int32_t n_phys[3], const double h[3], int npml, double freq, int unit,
-                  int nlevels, cudaStream_t st, MlPlan &plan)
+// Levels on the host: each level's grid (PML included) and FP64 wavenumber.
+int ml_levels_host(const double *v_phys, const int32_t n_phys[3], const double h[3], int npml, double freq, int unit,
+                   int nlevels, std::vector<h3d_grid> &grids, std::vector<std::vector<double>> &wn)
 {
     if (!v_phys || !n_phys || !h || npml < 0 || !(freq > 0.0) || nlevels < 1 || nlevels > 8) {
         set_error("multigrid set-up: bad argument");
@@ -237,16 +238,14 @@ int ml_plan_build(const double *v_phys, const int32_t n_phys[3], const double h[
         coarsen(vm[(size_t)i - 1], nm[(size_t)i - 1].data(), ns, vm[(size_t)i]);
     }
     // wavenumbers and grids
-    std::vector<std::vector<double>> wn((size_t)nlevels);
-    plan.nlevels = nlevels;
-    plan.lv.assign((size_t)nlevels, h3d_ml_level{});
-    std::vector<h3d_ml_level> &lv = plan.lv;
+    wn.assign((size_t)nlevels, std::vector<double>());
+    grids.assign((size_t)nlevels, h3d_grid{});
     for (int i = 0; i < nlevels; ++i) {
         const double s = std::ldexp(1.0, i);
         const int p = (int)std::ceil((double)npml / s);
         int32_t nt[3];
         wavenumber(vm[(size_t)i], nm[(size_t)i].data(), p, freq, unit, wn[(size_t)i], nt);
-        h3d_grid &g = lv[(size_t)i].grid;
+        h3d_grid &g = grids[(size_t)i];
         for (int a = 0; a < 3; ++a) {
             g.n[a] = nt[a];
             g.h[a] = h[a] * s;
@@ -254,6 +253,20 @@ int ml_plan_build(const double *v_phys, const int32_t n_phys[3], const double h[
         for (int a = 0; a < 6; ++a) g.npml[a] = p;
         if ((rc = check_grid(&g))) return rc;
     }
+    return H3D_OK;
+}
+
+int ml_plan_build(const double *v_phys, const int32_t n_phys[3], const double h[3], int npml, double freq, int unit,
+                  int nlevels, cudaStream_t st, MlPlan &plan)
+{
+    std::vector<h3d_grid> grids;
+    std::vector<std::vector<double>> wn;
+    int rc = ml_levels_host(v_phys, n_phys, h, npml, freq, unit, nlevels, grids, wn);
+    if (rc) return rc;
+    plan.nlevels = nlevels;
+    plan.lv.assign((size_t)nlevels, h3d_ml_level{});
+    std::vector<h3d_ml_level> &lv = plan.lv;
+    for (int i = 0; i < nlevels; ++i) lv[(size_t)i].grid = grids[(size_t)i];
     // transfers between neighbouring computational grids
     std::vector<Csr> Pc((size_t)3 * (nlevels - 1)), Rc((size_t)3 * (nlevels - 1));
     for (int i = 0; i + 1 < nlevels; ++i)
@@ -364,6 +377,32 @@ int h3d_ml_interp_weights(int kind, const double *xin, int nin, const double *xo
     if (kind == 0) linear_weights(xi, xo, W);
     else cubic_weights(xi, xo, W);
     std::copy(W.begin(), W.end(), A);
+    return H3D_OK;
+}
+
+int h3d_ml_levels_host(const double *v_phys, const int32_t n_phys[3], const double h[3], int npml, double freq,
+                       int unit, int nlevels, h3d_grid *grids, double *wn, size_t wn_cap)
+{
+    if (!grids || !wn) {
+        set_error("h3d_ml_levels_host: bad argument");
+        return H3D_ERR_BAD_ARG;
+    }
+    std::vector<h3d_grid> g;
+    std::vector<std::vector<double>> w;
+    int rc = ml_levels_host(v_phys, n_phys, h, npml, freq, unit, nlevels, g, w);
+    if (rc) return rc;
+    size_t need = 0;
+    for (const auto &x : w) need += x.size();
+    if (wn_cap < need) {
+        set_error("h3d_ml_levels_host: wn holds %zu values, the levels need %zu", wn_cap, need);
+        return H3D_ERR_BAD_ARG;
+    }
+    size_t off = 0;
+    for (int i = 0; i < nlevels; ++i) {
+        grids[i] = g[(size_t)i];
+        std::copy(w[(size_t)i].begin(), w[(size_t)i].end(), wn + off);
+        off += w[(size_t)i].size();
+    }
     return H3D_OK;
 }
 

@@ -141,6 +141,8 @@ _SIGS = {
     "h3d_ml_default_opts": (None, [C.POINTER(MLOpts)]),
     "h3d_ml_interp_weights": (C.c_int, [C.c_int, dp, C.c_int, dp, C.c_int, dp]),
     "h3d_ml_coarsen_model": (C.c_int, [dp, C.POINTER(C.c_int32), C.POINTER(C.c_int32), dp]),
+    "h3d_ml_levels_host": (C.c_int, [dp, C.POINTER(C.c_int32), dp, C.c_int, C.c_double, C.c_int, C.c_int,
+                                     C.POINTER(Grid), dp, C.c_size_t]),
     "h3d_mlgmres_solve_model": (C.c_int, [dp, C.POINTER(C.c_int32), dp, C.c_int, C.c_double, C.c_int, C.c_int, vp,
                                           vp, C.c_int, C.POINTER(MLOpts), dp, C.c_int, C.POINTER(MLInfo), vp]),
     "h3d_mex_mlgmres": (C.c_int, [dp, dp, C.c_size_t, dp, C.c_double, C.c_double, C.c_int, C.c_int, dp, dp,

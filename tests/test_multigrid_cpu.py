@@ -139,3 +139,41 @@ def test_library_levels_and_transfers_match_oracle():
         assert abs(sparse(P[i]) - sparse_o(Po[i])).max() <= 1e-14
         f2c, s = Ro[i]
         assert abs(sparse(R[i]) - s * sparse_o(f2c)).max() <= 1e-14
+
+
+def test_library_hierarchy_from_the_model_matches_oracle():
+    """h3d_ml_levels_host (what h3d_mlgmres_solve_model and the h3d_mlgmres_mex gateway build):
+    level grids, spacings, PML widths and wavenumbers against the oracle's construct_multigrid
+    restatement, in each model unit."""
+    import ctypes as C
+    import os
+    import sys
+
+    sys.path.insert(0, os.path.join(os.path.dirname(__file__), "..", "slim-release-apps_gb300"))
+    from h3d import _lib as L
+
+    lib = L.load()
+    rng = np.random.default_rng(11)
+    n, h, npml = (17, 15, 13), (25.0, 20.0, 30.0), 6
+    v = 1500.0 + 1000.0 * rng.random(n)
+    for unit, vv in (("m/s", v), ("s2/m2", v ** -2.0), ("s2/km2", 1e6 * v ** -2.0)):
+        ref, _, _ = ML.build_levels(vv, h, npml, 4.0, unit)
+        grids = (L.Grid * 3)()
+        wn = np.zeros(sum(lv.N for lv in ref))
+        src = np.ascontiguousarray(vv.reshape(-1, order="F"))
+        hh = np.asarray(h, float)
+        rc = lib.h3d_ml_levels_host(src.ctypes.data_as(L.dp), (C.c_int32 * 3)(*n), hh.ctypes.data_as(L.dp), npml,
+                                    4.0, L.UNITS[unit], 3, grids, wn.ctypes.data_as(L.dp), wn.size)
+        assert rc == L.OK
+        off = 0
+        for i, lv in enumerate(ref):
+            assert tuple(grids[i].n) == lv.nt
+            assert tuple(grids[i].h) == lv.dt
+            assert set(grids[i].npml) == {lv.npml}
+            w = wn[off:off + lv.N]
+            off += lv.N
+            assert np.max(np.abs(w - lv.wn)) <= 1e-12 * np.max(np.abs(lv.wn))
+    small = np.zeros(10)
+    rc = lib.h3d_ml_levels_host(src.ctypes.data_as(L.dp), (C.c_int32 * 3)(*n), hh.ctypes.data_as(L.dp), npml, 4.0,
+                                0, 3, grids, small.ctypes.data_as(L.dp), small.size)
+    assert rc == L.ERR_BAD_ARG and b"levels need" in lib.h3d_last_error()
