@@ -14,7 +14,9 @@ Reported (one JSON line on rank 0):
              double sweeps (x read and written per right-hand side, the wavenumber read once)
              over their device time, sampled live inside the timed solves by event nodes in the
              solver's CUDA graph
-  fp64       the same solve in plain FP64 (mixed-versus-FP64 speed-up, wavefield difference)
+  fp64       the same solve in plain FP64 (mixed-versus-FP64 speed-up, wavefield difference, and
+             its algorithmic FP64 flop rate against the nominal FP64 peak: that path is bound by
+             GB300's FP64 throughput, not by HBM)
   error_vs_fp64_oracle  both wavefields against the C oracle's FP64 solution of the same
              problem to a true residual of 1.1e-9 (tests/golden/config1_solve.npz)
   mlgmres    the same problem by FGMRES + the three-level ML_GMRES multigrid (the reference
@@ -57,6 +59,12 @@ sys.path.insert(0, os.path.join(ROOT, "slim-release-apps_gb300"))
 
 METRIC = "3D Helmholtz solves/s & FWI grads/s at 1e-6 resid: mixed batched vs FP64"
 WORKLOAD = "config1: 201x201x101 incl. 20-pt PML, h=20 m, 6 Hz, single surface source, 1e-6 true residual"
+# Algorithmic flops per grid point: a Kaczmarz double sweep (two passes of 27 complex
+# multiply-adds for the projection, 27 for the update and the row norm) and the CGMN vector work
+# of one iteration (two inner products and three updates in complex arithmetic).
+SWEEP_FLOP_PER_PT = 1040
+CG_FLOP_PER_PT = 40
+FP64_NOMINAL_TFLOPS = 1.25   # GB300 FP64 (nominal; the FP64 path is bound by it, not by HBM)
 
 # CGMN iterations the reference ordering (lexicographic Kaczmarz double sweep,
 # linearsolve.m:148-156 + CGMN.m) needs on the headline workload to reach a true relative
@@ -486,6 +494,10 @@ def run_gpu_arm(args, world, rank):
         fp64 = {"solves_per_s": 1.0 / t64, "ms_per_solve": 1e3 * t64, "iters": info64["iters"],
                 "mixed_speedup": (1.0 / (elapsed / args.steps)) / (1.0 / t64),
                 "wavefield_rel_diff_mixed_vs_fp64": diff, "rel_res_true": info64["rel_res_true"]}
+        tf = info64["iters"] * (SWEEP_FLOP_PER_PT + CG_FLOP_PER_PT) * N / t64 / 1e12
+        fp64["fp64_flop_rate"] = {"achieved_tflops": tf, "peak_tflops": FP64_NOMINAL_TFLOPS,
+                                  "frac": tf / FP64_NOMINAL_TFLOPS, "peak_source": "nominal",
+                                  "flop_per_pt_iter": SWEEP_FLOP_PER_PT + CG_FLOP_PER_PT}
     else:
         u64 = None
     # error of the wavefields against the FP64 oracle's solution of the same problem (true
