@@ -177,3 +177,139 @@ def test_library_hierarchy_from_the_model_matches_oracle():
     rc = lib.h3d_ml_levels_host(src.ctypes.data_as(L.dp), (C.c_int32 * 3)(*n), hh.ctypes.data_as(L.dp), npml, 4.0,
                                 0, 3, grids, small.ctypes.data_as(L.dp), small.size)
     assert rc == L.ERR_BAD_ARG and b"levels need" in lib.h3d_last_error()
+
+
+def _device_formulation_fgmres(A, b, tol, maxit, m, precond=None):
+    """The arithmetic h3d_mlgmres.cu runs, restated step by step on the CPU: classical
+    Gram-Schmidt; the new Givens rotation from reciprocal square roots (c = |a| / r,
+    s = (a / |a|) ||w|| / r, the quasi-residual carried as |s| times the previous one); an
+    unnormalised basis with one scale per vector when there is no preconditioner (vector 0 is
+    the residual itself); y back-substituted once per cycle; the stopping flags of the state
+    block (a step runs while the quasi-residual exceeds tol, a cycle ends with the true
+    residual's break test).  x0 = 0."""
+    n = b.size
+    lazy = precond is None
+    r = b.copy()
+    x = np.zeros_like(b)
+    normr0 = np.linalg.norm(r)
+    hst = [1.0]
+    live = normr0 != 0.0 and 1.0 > tol and (1 // m) < maxit
+    it = 1
+    for _ in range(maxit):
+        if not live:
+            break
+        beta = np.linalg.norm(r)
+        U = np.zeros((m + 1, n), complex)
+        sv = np.zeros(m + 1)
+        Z = np.zeros((m, n), complex)
+        cs = np.zeros(m)
+        sn = np.zeros(m, complex)
+        g = np.zeros(m + 1, complex)
+        R = np.zeros((m, m), complex)
+        g[0] = beta
+        gres = beta
+        if lazy:
+            U[0], sv[0] = r, 1.0 / beta
+        else:
+            U[0], sv[0] = r / beta, 1.0
+        k = 0
+        for j in range(m):
+            vj = sv[j] * U[j] if lazy else U[j]
+            if precond is not None:
+                Z[j] = precond(U[j])
+                w_raw = A(Z[j])
+            else:
+                w_raw = A(U[j])
+            raw = U[:j + 1].conj() @ w_raw
+            h = sv[:j + 1] * sv[j] * raw if lazy else raw
+            w = (sv[j] if lazy else 1.0) * w_raw - (U[:j + 1].T @ ((sv[:j + 1] if lazy else 1.0) * h))
+            w2 = float(np.vdot(w, w).real)
+            rhn = w2 ** -0.5 if w2 > 0 else 0.0
+            hn = w2 * rhn
+            c = h.astype(complex).copy()
+            for i in range(j):
+                t = cs[i] * c[i] + sn[i] * c[i + 1]
+                c[i + 1] = cs[i] * c[i + 1] - np.conj(sn[i]) * c[i]
+                c[i] = t
+            a = c[j]
+            na2 = abs(a) ** 2
+            if w2 == 0.0:
+                cj, sj, sabs, rjj = 1.0, 0.0, 0.0, a
+            elif na2 == 0.0:
+                cj, sj, sabs, rjj = 0.0, 1.0, 1.0, hn
+            else:
+                r2 = na2 + w2
+                rr, rna = r2 ** -0.5, na2 ** -0.5
+                ph = rna * a
+                cj, sabs = na2 * rna * rr, hn * rr
+                sj, rjj = sabs * ph, (r2 * rr) * ph
+            c[j] = rjj
+            cs[j], sn[j] = cj, sj
+            R[:j + 1, j] = c
+            g[j + 1] = -np.conj(sj) * g[j]
+            g[j] = cj * g[j]
+            gres = sabs * gres
+            q = gres / normr0
+            hst.append(q)
+            it += 1
+            k = j + 1
+            if j + 1 < m:
+                if lazy:
+                    U[j + 1], sv[j + 1] = w, rhn
+                else:
+                    U[j + 1], sv[j + 1] = w * rhn, 1.0
+            if not (q > tol and j + 1 < m):
+                break
+        y = np.zeros(k, complex)
+        for i in range(k - 1, -1, -1):
+            t = g[i] - R[i, i + 1:k] @ y[i + 1:k]
+            d = R[i, i]
+            y[i] = 0.0 if abs(d) == 0.0 else t / d
+        basis = Z[:k] if precond is not None else (sv[:k, None] * U[:k] if lazy else U[:k])
+        x = x + basis.T @ y
+        r = b - A(x)
+        rn = np.linalg.norm(r)
+        if rn / normr0 < tol:
+            live = False
+        else:
+            live = hst[-1] > tol and (it // m) < maxit
+    return x, np.array(hst)
+
+
+def test_device_fgmres_formulation_matches_oracle():
+    """The device formulation (reciprocal-square-root Givens rotations, unnormalised basis,
+    once-per-cycle back substitution, flag-driven stopping) gives FGMRES.m's iterates: same
+    quasi-residual history and solution as the oracle's restatement with numpy lstsq, with and
+    without a preconditioner, and through a breakdown (numerical and exact, ||w|| = 0)."""
+    rng = np.random.default_rng(21)
+    n = 30
+    A = (rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n))) / np.sqrt(n) + 1.5 * np.eye(n)
+    b = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    D = np.diag(1.0 + rng.random(n))
+    for m, maxit, tol in ((5, 3, 1e-30), (4, 6, 1e-8), (8, 2, 1e-4)):
+        for pre in (None, lambda v: D @ v):
+            x_ref, _, h_ref = ML.fgmres(lambda v: A @ v, b, None, tol=tol, maxit=maxit, maxinnerit=m,
+                                        precond=pre)
+            x, h = _device_formulation_fgmres(lambda v: A @ v, b, tol, maxit, m, precond=pre)
+            assert len(h) == len(h_ref)
+            np.testing.assert_allclose(h, h_ref, rtol=1e-9, atol=1e-14)
+            assert np.linalg.norm(x - x_ref) <= 1e-10 * np.linalg.norm(x_ref)
+    # b in a 3-dimensional invariant subspace: ||w|| falls to rounding level at step 3
+    Q, _ = np.linalg.qr(rng.standard_normal((n, n)) + 1j * rng.standard_normal((n, n)))
+    lam = np.concatenate([[2.0, 3.0 + 1j, 0.5 - 2j], 1.0 + rng.random(n - 3)])
+    Ab = Q @ np.diag(lam) @ Q.conj().T
+    bb = Q[:, :3] @ np.array([1.0, 2.0 - 1j, 0.5])
+    x, h = _device_formulation_fgmres(lambda v: Ab @ v, bb, 1e-12, 3, 5)
+    assert len(h) <= 5 and h[-1] <= 1e-10
+    assert np.linalg.norm(Ab @ x - bb) <= 1e-10 * np.linalg.norm(bb)
+    # exact breakdown (the ||w|| = 0 branch): b an eigenvector of a diagonal A
+    Ad = np.diag(np.arange(1.0, n + 1.0) * (1.0 + 0.5j))
+    e1 = np.zeros(n, complex)
+    e1[0] = 2.0
+    for pre in (None, lambda v: v):
+        x, h = _device_formulation_fgmres(lambda v: Ad @ v, e1, 1e-12, 3, 5, precond=pre)
+        with np.errstate(invalid="ignore", divide="ignore"):   # FGMRES.m:103 forms V(:,2) = 0/0, unused
+            x_ref, _, h_ref = ML.fgmres(lambda v: Ad @ v, e1, None, tol=1e-12, maxit=3, maxinnerit=5, precond=pre)
+        np.testing.assert_allclose(h, h_ref, atol=1e-15)
+        assert list(h) == [1.0, 0.0]
+        np.testing.assert_allclose(x, x_ref, rtol=1e-15)
