@@ -383,7 +383,8 @@ typedef enum { H3D_UNIT_M_PER_S = 0, H3D_UNIT_S2_PER_M2 = 1, H3D_UNIT_S2_PER_KM2
  * included; the call fails with H3D_ERR_BAD_ARG if it would overflow.  The control flow runs
  * on the host; the Arnoldi steps, Givens rotations and stopping tests on the device, so that
  * the host waits only before a step that applies the preconditioner and at the end of an
- * unpreconditioned cycle.  Synchronises `stream` before returning. */
+ * unpreconditioned cycle.  A non-finite residual (NaN or Inf in the data) returns
+ * H3D_ERR_NONFINITE after the loop stops.  Synchronises `stream` before returning. */
 int h3d_mlgmres_solve(const h3d_ml_level *levels, int nlevels, const h3d_ml_transfer *restrict_ops,
                       const h3d_ml_transfer *prolong_ops, const void *b, void *x, int mode,
                       const h3d_ml_opts *opts, double *hst, int hst_cap, h3d_ml_info *info,

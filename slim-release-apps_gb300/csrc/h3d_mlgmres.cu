@@ -35,6 +35,7 @@
 // The mixed precision of the Python front end carries over: the outer FGMRES in complex128,
 // the V-cycle (all levels, smoothers and coarse solves) in complex64 with FP64 inner products.
 #include <chrono>
+#include <cmath>
 #include <functional>
 
 #include "h3d_kernels.cuh"
@@ -498,7 +499,7 @@ __global__ void __launch_bounds__(kThr) fg_norm_kernel(FgState *st, const double
             h.live = 0;
             h.conv = 1;
         } else {
-            if (!(h.hst > tol)) h.conv = 1;
+            if (h.hst <= tol) h.conv = 1;  // (a NaN quasi-residual stops the loop unconverged)
             h.live = (h.hst > tol && cycles_left(h.it, m, maxit)) ? 1 : 0;
         }
     }
@@ -968,6 +969,10 @@ extern "C" int h3d_mlgmres_solve(const h3d_ml_level *levels, int nlevels, const 
         info->kernel_launches = R.launches;
         info->host_syncs = R.syncs;
         info->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    if (!std::isfinite(R.hh->hst) || !std::isfinite(R.hh->rn)) {
+        set_error("h3d_mlgmres_solve: non-finite residual (NaN or Inf in b, x or the wavenumbers)");
+        return H3D_ERR_NONFINITE;
     }
     return H3D_OK;
 }
